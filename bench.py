@@ -1,0 +1,433 @@
+"""Benchmark: integral-direct Fock build of a (H2O)_16 cluster in cc-pVDZ.
+
+One step = one Fock build F = H + J - K/2 of the seeded (H2O)_16 cluster
+(11 A cube, seed 16; 400 Cartesian basis functions) directly from the
+Schwarz-screened ERIs (threshold 1e-12), in mixed precision (quartets with
+Schwarz bound < 1e-4 in FP32 with FP64 Boys recursion; FP64 above), the
+headline configuration.  The FP64 plain build of the same workload is timed in
+the same run and reported beside it, with the SCF energy error of the mixed
+scheme against the FP64 SCF.
+
+Prints ONE JSON line (rank 0).  ``--impl reference`` times the reference's CPU
+algorithm (the oracle's C restatement of electronrepulsion.py, faithful loop
+structure, all host threads) on bounded samples of the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ERI quartets/s & Fock-build ms, mixed vs FP64 plain on GPU at |ΔE|≤1e-6 Eh"
+WATERS, BOX, SEED, BASIS = 16, 11.0, 16, "cc-pvdz"
+SCREEN, FP32_THR = 1e-12, 1e-4
+
+
+def workload_geometry() -> str:
+    from slowquant_gb300 import systems
+
+    return systems.water_cluster(WATERS, BOX, SEED)
+
+
+def config(extra=None) -> dict:
+    c = {
+        "workload": f"(H2O)_{WATERS} cc-pVDZ Fock build (J+K), 400 Cartesian bf, 11 A cube seed {SEED}",
+        "molecule": f"(H2O)_{WATERS}",
+        "basis": "cc-pVDZ (Cartesian, 400 bf)",
+        "schwarz_threshold": SCREEN,
+        "fp32_schwarz_threshold": FP32_THR,
+        "precision": "mixed (FP32 quartets below bound 1e-4, FP64 Boys recursion; FP64 above)",
+        "step": "one Fock build F = H + J - K/2 from a converged-SCF density",
+        "l2": "flushed between timed steps (512 MB write); quartet list > L2",
+        "parallelism": "replicas only",
+    }
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- helpers
+def measured_peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            return json.load(fh)
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+def fma_peak(lib, torch, precision: int) -> float:
+    """Measured FMA throughput (FLOP/s) of one pipe via the library's probe kernel."""
+    from slowquant_gb300 import _lib
+
+    blocks, iters = 152 * 8, (20000 if precision == _lib.SQ_FP64 else 400000)
+    out = torch.empty(blocks * 256, dtype=torch.float64, device="cuda")
+    s = _lib.stream_handle()
+    _lib.check(lib.sq_fma_probe(precision, blocks, 100, out.data_ptr(), s), "sq_fma_probe")
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _lib.check(lib.sq_fma_probe(precision, blocks, iters, out.data_ptr(), s), "sq_fma_probe")
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 16.0 * iters * 256 * blocks / (e0.elapsed_time(e1) * 1e-3))
+    return best
+
+
+def class_work(eng, ql) -> dict:
+    """Per quartet class: contracted quartets, primitive quartets, model FLOPs."""
+    import torch
+
+    from slowquant_gb300 import flops
+
+    npp = torch.tensor(eng.pair_np, dtype=torch.int64, device=eng.device)
+    out = {}
+    for c in range(21):
+        a, b = int(ql.class_off[c]), int(ql.class_off[c + 1])
+        if b == a:
+            continue
+        seg = ql.pairs[a:b].long()
+        nprim = int((npp[seg[:, 0]] * npp[seg[:, 1]]).sum())
+        la, lb, lc, ld = flops.quartet_class_l(c)
+        f = nprim * flops.flops_per_primitive_quartet(la, lb, lc, ld) + (b - a) * flops.flops_per_contracted_quartet_jk(
+            la, lb, lc, ld)
+        out[c] = {"quartets": b - a, "prim_quartets": nprim, "flops": float(f), "class": f"{la}{lb}{lc}{ld}"}
+    return out
+
+
+def time_events(torch, fn, n: int, flush=None) -> list[float]:
+    ts = []
+    for _ in range(n):
+        if flush is not None:
+            flush()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return ts
+
+
+# ----------------------------------------------------------------- CPU arm
+def cpu_sample(eng_or_none, target_seconds: float, seed: int = 0, pairs_host=None, mol_geom=None):
+    """Time the oracle (faithful restatement of the reference) on random surviving quartets."""
+    from oracle import oracle as O
+
+    o = O.OracleMolecule(mol_geom, BASIS, "angstrom")
+    rng = np.random.default_rng(seed)
+    pair_shells, quartets = pairs_host
+    nthreads = os.cpu_count() or 1
+    # calibrate on a small sample, then size the timed sample
+    n = 64
+    while True:
+        idx = rng.integers(0, len(quartets), n)
+        sq = np.concatenate([pair_shells[quartets[idx, 0]], pair_shells[quartets[idx, 1]]], axis=1)
+        t0 = time.time()
+        o.eri_quartets(sq, nthreads=nthreads, faithful=True)
+        dt = time.time() - t0
+        if dt > 0.3 * target_seconds or n >= 2_000_000:
+            return n / dt, nthreads, n, dt
+        n = int(n * min(16.0, max(2.0, 0.5 * target_seconds / max(dt, 1e-3))))
+
+
+def reference_arm(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    # Build the workload's screened quartet list on the host (the oracle's own Schwarz factors).
+    from oracle import oracle as O
+    from slowquant_gb300 import screening
+    from slowquant_gb300.molecule import _Molecule
+
+    geom = workload_geometry()
+    m = _Molecule(geom, 0, "angstrom")
+    m._set_basis_set(BASIS)
+    o = O.OracleMolecule(geom, BASIS, "angstrom")
+    cs = o.schwarz(nthreads=os.cpu_count() or 1)
+    pair_shells, pc, npa, npb, q = _host_pairs(m, cs)
+    lists, ket = screening.build_tasks(pc, npa, npb, q, SCREEN)
+    quartets = screening.expand_host(*screening.flatten_tasks(lists[0])[:3], ket)
+    rates = []
+    t_start = time.time()
+    for step in range(args.warmup + args.steps):
+        rate, nthreads, n, dt = cpu_sample(None, args.cpu_seconds, seed=step, pairs_host=(pair_shells, quartets),
+                                           mol_geom=geom)
+        if step >= args.warmup:
+            rates.append(rate)
+    value = float(np.median(rates))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "quartets/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": len(quartets) / value * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config({"total_quartets": len(quartets)}),
+        "cpu_baseline": {"value": value, "unit": "quartets/s", "cores": os.cpu_count() or 1, "kind": "port",
+                         "sample": f"per step ~{args.cpu_seconds:.0f} s of uniformly random surviving unique shell "
+                                   f"quartets of the workload through the oracle's faithful C restatement of "
+                                   f"electron_repulsion_integral (ms_per_step extrapolates to the full "
+                                   f"{len(quartets)}-quartet build)"},
+        "e2e": {"value": value, "unit": "quartets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": round(time.time() - t_start, 1),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _host_pairs(m, cs):
+    """Pair table in the engine's order (host restatement, for the CPU arm)."""
+    from slowquant_gb300 import screening  # noqa: F401
+
+    l = np.array([s.angular_momentum for s in m.shells])
+    nprim = np.array([len(s.exponents) for s in m.shells])
+    i, j = np.triu_indices(len(l))
+    a = np.where(l[i] >= l[j], i, j)
+    b = np.where(l[i] >= l[j], j, i)
+    pc = l[a] * (l[a] + 1) // 2 + l[b]
+    order = np.argsort(pc, kind="stable")
+    a, b, pc = a[order], b[order], pc[order]
+    return np.stack([a, b], 1).astype(np.int32), pc, nprim[a], nprim[b], cs[a, b]
+
+
+# ----------------------------------------------------------------- GPU arm
+def gpu_arm(args) -> None:
+    import torch
+    import torch.distributed as dist
+
+    from slowquant_gb300 import _lib
+    from slowquant_gb300.engine import IntegralEngine, QuartetList
+    from slowquant_gb300.hartreefock import DirectJK, run_hartree_fock
+    from slowquant_gb300.logger import _Logger
+    from slowquant_gb300.molecule import _Molecule
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    lib = _lib.lib()
+
+    geom = workload_geometry()
+    mol = _Molecule(geom, 0, "angstrom")
+    mol._set_basis_set(BASIS)
+    t0 = time.time()
+    eng = IntegralEngine(mol)
+    q_all = eng.quartets(SCREEN)
+    q64, q32 = eng.quartets(SCREEN, FP32_THR)
+    S, T, V = eng.one_electron()
+    H = T + V
+    torch.cuda.synchronize()
+    setup_s = time.time() - t0
+
+    # SCF in FP64 and in mixed precision: energies and the converged density
+    log = _Logger()
+    log.print_output = False
+    ne = mol.number_electrons
+    jk64 = DirectJK(eng, SCREEN, "fp64")
+    t0 = time.time()
+    E64, C64, F64, D64 = run_hartree_fock(S, T, V, jk64, ne, log, 1e-9, 1e-9, 100, True)
+    scf64_s = time.time() - t0
+    jkm = DirectJK(eng, SCREEN, "mixed", FP32_THR, 1e-5)
+    t0 = time.time()
+    Em, _, _, _ = run_hartree_fock(S, T, V, jkm, ne, log, 1e-9, 1e-9, 100, True)
+    scfm_s = time.time() - t0
+    n_mixed_builds = sum(1 for b in jkm.builds if b != "fp64")
+    D = torch.tensor(D64, dtype=torch.float64, device="cuda")
+
+    flush_buf = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def flush():
+        flush_buf.zero_()
+
+    def step_mixed():
+        eng.fock(H, D, SCREEN, "mixed", FP32_THR)
+
+    def step_fp64():
+        eng.fock(H, D, SCREEN, "fp64")
+
+    for _ in range(args.warmup):
+        step_mixed()
+        step_fp64()
+    torch.cuda.synchronize()
+
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_wall = time.time()
+        ms_mixed = time_events(torch, step_mixed, args.steps, flush)
+        wall_mixed = time.time() - t_wall
+    ms_fp64 = time_events(torch, step_fp64, max(3, min(args.steps, 5)), flush)
+    torch.cuda.synchronize()
+    tot_mixed = sum(ms_mixed)
+    if world > 1:
+        t = torch.tensor([tot_mixed], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_mixed = float(t.item())
+
+    ms_step = tot_mixed / args.steps
+    nq = q_all.nquartet
+    value = world * nq / (ms_step * 1e-3)
+    ms64 = float(np.median(ms_fp64))
+
+    # e2e through the public API: pinned host D -> device, Fock build, F -> pinned host
+    D_host = torch.empty_like(D, device="cpu").pin_memory()
+    D_host.copy_(D)
+    F_host = torch.empty_like(D_host).pin_memory()
+
+    def step_e2e():
+        Dd = D_host.to("cuda", non_blocking=True)
+        F = eng.fock(H, Dd, SCREEN, "mixed", FP32_THR)
+        F_host.copy_(F, non_blocking=True)
+
+    for _ in range(2):
+        step_e2e()
+    ms_e2e = time_events(torch, step_e2e, args.steps, flush)
+    e2e_ms = float(np.mean(ms_e2e))
+
+    # roofline of the dominant kernel (per-class launches timed alone)
+    peak64 = fma_peak(lib, torch, _lib.SQ_FP64)
+    peak32 = fma_peak(lib, torch, _lib.SQ_FP32)
+    work64 = class_work(eng, q64)
+    work32 = class_work(eng, q32)
+    work_all = class_work(eng, q_all)
+    rows = []
+    for lst, prec, work in ((q64, "fp64", work64), (q32, "fp32", work32)):
+        for c, w in work.items():
+            off = np.zeros(22, dtype=np.int64)
+            off[c + 1:] = w["quartets"]
+            sub = QuartetList(lst.pairs[lst.class_off[c]:lst.class_off[c + 1]], off)
+            eng.jk_accumulate(D, [sub], [prec])
+            t = float(np.median(time_events(torch, lambda: eng.jk_accumulate(D, [sub], [prec]), 3, flush)))
+            rows.append({"class": w["class"], "precision": prec, "ms": t, "flops": w["flops"],
+                         "quartets": w["quartets"]})
+    rows.sort(key=lambda r: -r["ms"])
+    dom = rows[0]
+    # The J/K launch also zeroes two nbf^2 accumulators (negligible at 400 bf).
+    peak = peak64 if dom["precision"] == "fp64" else peak32
+    achieved = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
+    fl64 = sum(w["flops"] for w in work_all.values())
+    launches = sum(1 for c in range(21) if q64.class_off[c + 1] > q64.class_off[c]) + sum(
+        1 for c in range(21) if q32.class_off[c + 1] > q32.class_off[c]) + 2
+
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "quartets/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32 (mixed)", "data": "synthetic",
+        "config": config({"nbf": eng.nbf, "surviving_quartets": nq, "fp64_quartets": q64.nquartet,
+                          "fp32_quartets": q32.nquartet}),
+        "fock_build_ms": {"mixed": ms_step, "fp64": ms64, "speedup_mixed_vs_fp64": ms64 / ms_step},
+        "quartets_per_s": {"mixed": nq / (ms_step * 1e-3), "fp64": nq / (ms64 * 1e-3)},
+        "energy": {"E_hf_fp64": E64, "E_hf_mixed": Em, "abs_dE_mixed_vs_fp64": abs(Em - E64),
+                   "mixed_builds": n_mixed_builds, "total_builds_mixed": len(jkm.builds),
+                   "scf_iterations_fp64": len(jk64.builds), "scf_s_fp64": round(scf64_s, 2),
+                   "scf_s_mixed": round(scfm_s, 2)},
+        "e2e": {"value": world * nq / (e2e_ms * 1e-3), "unit": "quartets/s",
+                "h2d_bytes_per_step": int(D.numel() * 8), "d2h_bytes_per_step": int(D.numel() * 8),
+                "ms_per_step": e2e_ms},
+        "roofline": {"bound": "fp64" if dom["precision"] == "fp64" else "fp32",
+                     "kernel": f"J/K class ({dom['class'][0]}{dom['class'][1]}|{dom['class'][2]}{dom['class'][3]}) "
+                               f"{dom['precision']}",
+                     "achieved": achieved, "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / (peak / 1e12),
+                     "peak_source": "measured by sq_fma_probe (FMA loop) in this run",
+                     "traffic": None, "flops_per_launch": dom["flops"], "ms_per_launch": dom["ms"]},
+        "roofline_fp64_build": {"flops": fl64, "ms": ms64, "achieved_tflops": fl64 / (ms64 * 1e-3) / 1e12,
+                                "peak_tflops": peak64 / 1e12, "frac": fl64 / (ms64 * 1e-3) / peak64},
+        "kernels_by_time": rows[:8],
+        "gpu_launches": launches * args.steps,
+        "clocks": clocks,
+        "setup_s": round(setup_s, 2),
+        "wall_timed_s": round(wall_mixed, 3),
+        "hbm_peak_gbs": measured_peaks().get("hbm_gbs"),
+    }
+    if rank == 0 and not args.no_cpu:
+        pairs_host = (eng.pair_shells, q_all.pairs[: q_all.nquartet].cpu().numpy())
+        rate, nthreads, n, dt = cpu_sample(None, args.cpu_seconds, 0, pairs_host, geom)
+        line["cpu_baseline"] = {
+            "value": rate, "unit": "quartets/s", "cores": nthreads, "kind": "port",
+            "sample": f"{n} uniformly random surviving unique shell quartets of the workload "
+                      f"({dt:.1f} s) through the oracle's faithful C restatement of electron_repulsion_integral"}
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,173 @@
+/*
+ * slowquant_gb300.h -- C ABI of the GB300 integral / Fock-build library.
+ *
+ * Every pointer inside the structs and every array argument is DEVICE memory
+ * owned by the caller, unless the comment says "host".  Every entry point is
+ * asynchronous on the given CUDA stream (a cudaStream_t passed as void*; NULL
+ * is the legacy default stream) and returns an int status:
+ *   SQ_OK (0) success, or one of the SQ_ERR_* codes below;
+ * sq_last_error() returns a human-readable message for the calling thread's
+ * last failure.  No entry point allocates device memory except where stated.
+ *
+ * The Python package (slowquant_gb300) binds these through ctypes and keeps
+ * the reference's entry points (SlowQuant, _Integral, run_hartree_fock, DIIS)
+ * on top of them.  Paths in the comments are relative to the SlowQuant
+ * project.
+ */
+#ifndef SLOWQUANT_GB300_H
+#define SLOWQUANT_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SQ_OK 0
+#define SQ_ERR_ARG 1          /* null pointer, bad size or inconsistent description */
+#define SQ_ERR_UNSUPPORTED 2  /* angular momentum beyond the compiled kernels */
+#define SQ_ERR_CUDA 3         /* CUDA launch or runtime error */
+#define SQ_ERR_NONFINITE 4    /* NaN or Inf found in an output */
+
+#define SQ_MAX_L 2            /* highest shell angular momentum (d) of the ERI kernels */
+#define SQ_MAX_QCLASS 21      /* quartet classes for l <= SQ_MAX_L: 6 pair classes -> 21 */
+
+/* Boys-function grid: F_m(T_k), T_k = k / SQ_BOYS_STEP_INV, k < SQ_BOYS_NGRID,
+ * m < SQ_BOYS_NCOL - 1; column SQ_BOYS_NCOL-1 holds exp(-T_k). */
+#define SQ_BOYS_NGRID 580
+#define SQ_BOYS_STEP_INV 16
+#define SQ_BOYS_NCOL 16
+#define SQ_BOYS_TMAX 36.0
+
+/* Precision of one ERI / J-K launch. */
+#define SQ_FP64 0             /* all arithmetic in FP64 */
+#define SQ_FP32 1             /* FP32 integral arithmetic, FP64 Boys downward recursion */
+#define SQ_FP32_BOYS32 2      /* FP32 integral arithmetic and FP32 Boys function */
+
+/* Contracted Cartesian Gaussian shells of one molecule (device arrays).
+ * Replaces the per-shell Python objects of slowquant/molecule/moleculeclass.py:269-301. */
+typedef struct sq_basis {
+    int nshell;
+    int nbf;
+    int natom;
+    int nprim_total;
+    const double *center;      /* [nshell][3], bohr */
+    const int *l;              /* [nshell] angular momentum */
+    const int *nprim;          /* [nshell] */
+    const int *prim_off;       /* [nshell] first primitive of the shell */
+    const int *bf_off;         /* [nshell] first basis function of the shell */
+    const double *exps;        /* [nprim_total] Gaussian exponents */
+    const double *coefs;       /* [nprim_total] contraction coefficient x the component-independent
+                                  part of the normalisation; the per-component factor
+                                  1/sqrt((2x-1)!!(2y-1)!!(2z-1)!!) is applied by the kernels */
+    const double *atom_xyz;    /* [natom][3], bohr */
+    const double *atom_charge; /* [natom] */
+} sq_basis;
+
+/* Shell pairs and their primitive-pair (Hermite) data.  The caller fills the
+ * index arrays and allocates the data arrays; sq_pair_prep writes them. */
+typedef struct sq_pairs {
+    int npair;
+    int nprimpair;
+    const int *shells;         /* [npair][2] shells (a, b) with l[a] >= l[b] */
+    const int *pp_off;         /* [npair+1] primitive-pair offsets */
+    const long long *herm_off; /* [npair] offset of the pair's first Hermite E value */
+    double *prim;              /* [nprimpair][8]: p, Px, Py, Pz, U, 0, 0, 0 (U = c_a c_b exp(-mu AB^2) / p) */
+    double *herm;              /* Hermite-expanded E^{ab}_{tuv}, x per-component normalisation */
+    float *prim32;             /* optional FP32 copy of prim (NULL: not written) */
+    float *herm32;             /* optional FP32 copy of herm */
+} sq_pairs;
+
+/* Shell-quartet work list: device array of (bra pair, ket pair) index pairs,
+ * grouped by quartet class; class_off (host) delimits each class segment.
+ * Quartet class of pair classes cb >= ck is cb*(cb+1)/2 + ck. */
+typedef struct sq_quartets {
+    long long nquartet;
+    const int *pairs;                        /* [nquartet][2] */
+    long long class_off[SQ_MAX_QCLASS + 1];  /* host */
+} sq_quartets;
+
+/* Library version and last error. */
+int sq_version(void);
+const char *sq_last_error(void);
+
+/* Process-wide tuning options (no reference counterpart).
+ * SQ_OPT_GENERIC_MIN_L: quartet classes with la+lb+lc+ld >= value run on the
+ * generic warp-cooperative kernel, the others on the per-class unrolled
+ * kernels (default 5; 0 sends every class to the generic kernel). */
+#define SQ_OPT_GENERIC_MIN_L 1
+int sq_set_option(int key, long long value);
+long long sq_get_option(int key);
+
+/* Fill the FP64 Boys grid table (SQ_BOYS_NGRID x SQ_BOYS_NCOL doubles) and,
+ * if table32 != NULL, its FP32 copy.  Replaces nothing: the reference
+ * evaluates boys_function by series on every call
+ * (slowquant/molecularintegrals/integralfunctions.py:74-97). */
+int sq_boys_table(double *table64, float *table32, void *stream);
+
+/* F_0..F_{n_max}(z[i]) for nz arguments -> out[nz][n_max+1].  Test hook for
+ * boys_function (integralfunctions.py:74-97). */
+int sq_boys(int n_max, const double *z, long long nz, const double *table64, double *out, void *stream);
+
+/* Primitive-pair data for every pair in `pairs`: P, p, U and the Hermite
+ * expansion coefficients of expansion_coefficients
+ * (integralfunctions.py:9-71), times the per-component normalisation of
+ * Shell.normalization (moleculeclass.py:292-299). */
+int sq_pair_prep(const sq_basis *basis, sq_pairs *pairs, void *stream);
+
+/* q[P] = sqrt(max over the (ab|ab) block) for every diagonal quartet (P, P)
+ * listed in `diagonal`: the shell-pair Cauchy-Schwarz matrix of
+ * get_cauchy_schwarz_matrix (slowquant/molecularintegrals/electronrepulsion.py:
+ * 300-339). */
+int sq_schwarz(const sq_basis *basis, const sq_pairs *pairs, const sq_quartets *diagonal, const double *table64,
+               double *q, void *stream);
+
+/* Dense ERI tensor V[nbf^4] (C order) from the quartets of `quartets`, each
+ * block scattered to its eight index permutations: the output of
+ * electron_repulsion_integral_driver (electronrepulsion.py:11-104).  V must be
+ * zeroed by the caller. */
+int sq_eri_dense(const sq_basis *basis, const sq_pairs *pairs, const sq_quartets *quartets,
+                 const double *table64, double *V, void *stream);
+
+/* Integral-direct Coulomb / exchange build: for the unique quartets of
+ * `quartets`, accumulate into Jacc/Kacc ([nbf][nbf], FP64, caller zeroes)
+ * so that sym(Jacc) = J = einsum("pqrs,sr->pq", ERI, D) and
+ * sym(Kacc) = K = einsum("psqr,sr->pq", ERI, D), the two einsums of
+ * run_hartree_fock (slowquant/hartreefock/hartreefock_in_memory.py:55-56).
+ * precision is SQ_FP64, SQ_FP32 or SQ_FP32_BOYS32; FP32 launches accumulate
+ * each quartet's FP32 contributions into the FP64 Jacc/Kacc.  D32 is caller
+ * scratch of nbf*nbf floats that FP32 launches fill with (float)D (unused,
+ * may be NULL, for SQ_FP64); FP32 launches need pairs->prim32/herm32 and
+ * table32. */
+int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_quartets *quartets, const double *table64,
+          const float *table32, const double *D, float *D32, double *Jacc, double *Kacc, int precision,
+          void *stream);
+
+/* F = H + J - K/2 with J = (Jacc + Jacc^T)/2, K = (Kacc + Kacc^T)/2
+ * (hartreefock_in_memory.py:57); J and K may be NULL. */
+int sq_fock_build(int nbf, const double *H, const double *Jacc, const double *Kacc, double *F, double *J,
+                  double *K, void *stream);
+
+/* One-electron matrices S, T, V ([nbf][nbf]; any may be NULL): overlap
+ * (multipole.py:48-135 with moment 0), kinetic energy (kineticenergy.py:42-133)
+ * and nuclear attraction (nuclearattraction.py:47-135). */
+int sq_one_electron(const sq_basis *basis, const double *table64, double *S, double *T, double *V,
+                    void *stream);
+
+/* Expand per-bra-pair tasks into the flat quartet list: task i writes
+ * (bra[i], ket_list[ket_start[i] + k]) for k < count[i] at out[offset[i] + k].
+ * offset is the exclusive prefix sum of count.  Replaces the shell-quartet
+ * loops and the Schwarz skip of electronrepulsion.py:32-49. */
+int sq_quartets_expand(long long ntask, const int *bra, const int *ket_start, const int *count,
+                       const long long *offset, const int *ket_list, int *out_pairs, long long nquartet,
+                       void *stream);
+
+/* Arithmetic-pipe probe (no reference counterpart): blocks x 256 threads each
+ * run `iters` iterations of 8 independent FMA chains in FP64 (precision
+ * SQ_FP64) or FP32 (otherwise), i.e. 16 * iters * 256 * blocks FLOPs; out
+ * holds blocks*256 elements of that type.  Timing it gives the measured FMA
+ * peak used as the roofline denominator of the FP64/FP32-pipe-bound kernels. */
+int sq_fma_probe(int precision, int blocks, int iters, void *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SLOWQUANT_GB300_H */

@@ -1,0 +1,112 @@
+"""ctypes binding of the C ABI declared in include/slowquant_gb300.h.
+
+The shared library ``libsqgb300.so`` is built in-tree by
+``slowquant_gb300.build``.  There is no fallback: if the library is missing or
+no CUDA device is present, every entry point raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsqgb300.so")
+
+SQ_OK = 0
+SQ_MAX_L = 2
+SQ_MAX_QCLASS = 21
+SQ_BOYS_NGRID = 580
+SQ_BOYS_STEP_INV = 16
+SQ_BOYS_NCOL = 16
+SQ_BOYS_TMAX = 36.0
+SQ_FP64 = 0
+SQ_FP32 = 1
+SQ_FP32_BOYS32 = 2
+SQ_OPT_GENERIC_MIN_L = 1
+
+PRECISIONS = {"fp64": SQ_FP64, "fp32": SQ_FP32, "fp32_boys32": SQ_FP32_BOYS32}
+
+_p = ctypes.c_void_p
+
+
+class SqBasis(ctypes.Structure):
+    _fields_ = [
+        ("nshell", ctypes.c_int), ("nbf", ctypes.c_int), ("natom", ctypes.c_int), ("nprim_total", ctypes.c_int),
+        ("center", _p), ("l", _p), ("nprim", _p), ("prim_off", _p), ("bf_off", _p), ("exps", _p),
+        ("coefs", _p), ("atom_xyz", _p), ("atom_charge", _p),
+    ]
+
+
+class SqPairs(ctypes.Structure):
+    _fields_ = [
+        ("npair", ctypes.c_int), ("nprimpair", ctypes.c_int), ("shells", _p), ("pp_off", _p),
+        ("herm_off", _p), ("prim", _p), ("herm", _p), ("prim32", _p), ("herm32", _p),
+    ]
+
+
+class SqQuartets(ctypes.Structure):
+    _fields_ = [
+        ("nquartet", ctypes.c_longlong), ("pairs", _p),
+        ("class_off", ctypes.c_longlong * (SQ_MAX_QCLASS + 1)),
+    ]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load libsqgb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build the CUDA library first "
+                "(python -m slowquant_gb300.build); there is no CPU fallback"
+            )
+        L = ctypes.CDLL(LIB_PATH)
+        L.sq_last_error.restype = ctypes.c_char_p
+        L.sq_version.restype = ctypes.c_int
+        L.sq_get_option.restype = ctypes.c_longlong
+        L.sq_get_option.argtypes = [ctypes.c_int]
+        L.sq_set_option.argtypes = [ctypes.c_int, ctypes.c_longlong]
+        L.sq_boys_table.argtypes = [_p, _p, _p]
+        L.sq_boys.argtypes = [ctypes.c_int, _p, ctypes.c_longlong, _p, _p, _p]
+        L.sq_pair_prep.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), _p]
+        L.sq_schwarz.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqQuartets), _p,
+                                 _p, _p]
+        L.sq_eri_dense.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqQuartets),
+                                   _p, _p, _p]
+        L.sq_jk.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqQuartets), _p, _p,
+                            _p, _p, _p, _p, ctypes.c_int, _p]
+        L.sq_fock_build.argtypes = [ctypes.c_int, _p, _p, _p, _p, _p, _p, _p]
+        L.sq_one_electron.argtypes = [ctypes.POINTER(SqBasis), _p, _p, _p, _p, _p]
+        L.sq_quartets_expand.argtypes = [ctypes.c_longlong, _p, _p, _p, _p, _p, _p, ctypes.c_longlong, _p]
+        L.sq_fma_probe.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _p, _p]
+        _lib = L
+    return _lib
+
+
+EXPORTED = [
+    "sq_version", "sq_last_error", "sq_set_option", "sq_get_option", "sq_boys_table", "sq_boys",
+    "sq_pair_prep", "sq_schwarz", "sq_eri_dense", "sq_jk", "sq_fock_build", "sq_one_electron",
+    "sq_quartets_expand", "sq_fma_probe",
+]
+
+
+def check(rc: int, what: str = "") -> None:
+    """Raise RuntimeError carrying sq_last_error() when rc != SQ_OK."""
+    if rc != SQ_OK:
+        msg = lib().sq_last_error().decode(errors="replace")
+        raise RuntimeError(f"slowquant_gb300 {what} failed (status {rc}): {msg}")
+
+
+def ptr(t) -> int | None:
+    """Device pointer of a torch tensor (None for None)."""
+    return None if t is None else t.data_ptr()
+
+
+def stream_handle(device=None) -> int:
+    import torch
+
+    return torch.cuda.current_stream(device).cuda_stream

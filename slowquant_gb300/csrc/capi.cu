@@ -1,0 +1,164 @@
+// capi.cu -- extern "C" entry points of the ERI / J-K kernels and the error state.
+#include <cstdarg>
+#include <cstdio>
+
+#include "capi_internal.cuh"
+#include "eri.cuh"
+#include "eri_warp.cuh"
+
+namespace sq {
+
+static thread_local char g_err[512] = "";
+
+int set_error(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int check_launch(const char *what) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(SQ_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    return SQ_OK;
+}
+
+#define DECL(QC) cudaError_t launch_qc_##QC(const EriArgs &, int, int, cudaStream_t);
+DECL(0) DECL(1) DECL(2) DECL(3) DECL(4) DECL(5) DECL(6) DECL(7) DECL(8) DECL(9) DECL(10) DECL(11)
+#undef DECL
+
+// Per-thread (fully unrolled) J/K kernels exist for the light classes (L <= 4,
+// except (dd|ss)); every other class, and every dense-tensor or Schwarz launch,
+// runs on the generic warp kernel.
+static const eri_launcher kLaunchers[SQ_MAX_QCLASS] = {
+    launch_qc_0, launch_qc_1, launch_qc_2, launch_qc_3, launch_qc_4, launch_qc_5, launch_qc_6,
+    launch_qc_7, launch_qc_8, launch_qc_9, launch_qc_10, launch_qc_11, nullptr, nullptr,
+    nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+};
+
+// Angular momenta of pair class pc (la >= lb).
+static void pair_class_l(int pc, int &la, int &lb) {
+    la = 0;
+    while ((la + 1) * (la + 2) / 2 <= pc) ++la;
+    lb = pc - la * (la + 1) / 2;
+}
+
+static void quartet_class_l(int qc, int &la, int &lb, int &lc, int &ld) {
+    int cb = 0;
+    while ((cb + 1) * (cb + 2) / 2 <= qc) ++cb;
+    const int ck = qc - cb * (cb + 1) / 2;
+    pair_class_l(cb, la, lb);
+    pair_class_l(ck, lc, ld);
+}
+
+// Classes with la+lb+lc+ld >= g_generic_min_l use the warp kernel.
+static int g_generic_min_l = 5;
+
+static int check_common(const char *who, const sq_basis *basis, const sq_pairs *pairs, const sq_quartets *qs,
+                        const double *tab) {
+    if (!basis || !pairs || !qs || !tab) return set_error(SQ_ERR_ARG, "%s: NULL argument", who);
+    if (!pairs->prim || !pairs->herm || !pairs->pp_off || !pairs->herm_off || !pairs->shells)
+        return set_error(SQ_ERR_ARG, "%s: pair data not allocated", who);
+    if (qs->nquartet < 0 || qs->class_off[0] != 0 || qs->class_off[SQ_MAX_QCLASS] != qs->nquartet)
+        return set_error(SQ_ERR_ARG, "%s: quartet class offsets inconsistent", who);
+    for (int c = 0; c < SQ_MAX_QCLASS; ++c)
+        if (qs->class_off[c + 1] < qs->class_off[c])
+            return set_error(SQ_ERR_ARG, "%s: quartet class offsets not ascending", who);
+    if (qs->nquartet > 0 && !qs->pairs) return set_error(SQ_ERR_ARG, "%s: quartet list is NULL", who);
+    return SQ_OK;
+}
+
+static int run_classes(const char *who, EriArgs args, const sq_quartets *qs, int mode, int precision,
+                       cudaStream_t stream) {
+    for (int c = 0; c < SQ_MAX_QCLASS; ++c) {
+        const long long n = qs->class_off[c + 1] - qs->class_off[c];
+        if (n == 0) continue;
+        args.quartets = reinterpret_cast<const int2 *>(qs->pairs) + qs->class_off[c];
+        args.nq = n;
+        int la, lb, lc, ld;
+        quartet_class_l(c, la, lb, lc, ld);
+        cudaError_t e;
+        if (mode != MODE_JK || la + lb + lc + ld >= g_generic_min_l || kLaunchers[c] == nullptr)
+            e = launch_eri_warp(args, WarpClass{la, lb, lc, ld}, mode, precision, stream);
+        else
+            e = kLaunchers[c](args, mode, precision, stream);
+        if (e != cudaSuccess) return set_error(SQ_ERR_CUDA, "%s: class %d: %s", who, c, cudaGetErrorString(e));
+    }
+    return SQ_OK;
+}
+
+}  // namespace sq
+
+using namespace sq;
+
+extern "C" int sq_version(void) { return 1; }
+
+extern "C" const char *sq_last_error(void) { return g_err; }
+
+extern "C" int sq_set_option(int key, long long value) {
+    if (key == SQ_OPT_GENERIC_MIN_L) {
+        if (value < 0) return set_error(SQ_ERR_ARG, "sq_set_option: negative L");
+        g_generic_min_l = (int)value;
+        return SQ_OK;
+    }
+    return set_error(SQ_ERR_ARG, "sq_set_option: unknown key %d", key);
+}
+
+extern "C" long long sq_get_option(int key) {
+    if (key == SQ_OPT_GENERIC_MIN_L) return g_generic_min_l;
+    return -1;
+}
+
+extern "C" int sq_schwarz(const sq_basis *basis, const sq_pairs *pairs, const sq_quartets *diagonal,
+                          const double *table64, double *q, void *stream) {
+    int rc = check_common("sq_schwarz", basis, pairs, diagonal, table64);
+    if (rc) return rc;
+    if (!q) return set_error(SQ_ERR_ARG, "sq_schwarz: q is NULL");
+    EriArgs a{};
+    a.basis = *basis;
+    a.pairs = *pairs;
+    a.tab64 = table64;
+    a.q = q;
+    return run_classes("sq_schwarz", a, diagonal, MODE_SCHWARZ, SQ_FP64, (cudaStream_t)stream);
+}
+
+extern "C" int sq_eri_dense(const sq_basis *basis, const sq_pairs *pairs, const sq_quartets *quartets,
+                            const double *table64, double *V, void *stream) {
+    int rc = check_common("sq_eri_dense", basis, pairs, quartets, table64);
+    if (rc) return rc;
+    if (!V) return set_error(SQ_ERR_ARG, "sq_eri_dense: V is NULL");
+    EriArgs a{};
+    a.basis = *basis;
+    a.pairs = *pairs;
+    a.tab64 = table64;
+    a.V = V;
+    return run_classes("sq_eri_dense", a, quartets, MODE_DENSE, SQ_FP64, (cudaStream_t)stream);
+}
+
+extern "C" int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_quartets *quartets,
+                     const double *table64, const float *table32, const double *D, float *D32, double *Jacc,
+                     double *Kacc, int precision, void *stream) {
+    int rc = check_common("sq_jk", basis, pairs, quartets, table64);
+    if (rc) return rc;
+    if (!D || !Jacc || !Kacc) return set_error(SQ_ERR_ARG, "sq_jk: D, Jacc and Kacc are required");
+    if (precision != SQ_FP64 && precision != SQ_FP32 && precision != SQ_FP32_BOYS32)
+        return set_error(SQ_ERR_ARG, "sq_jk: unknown precision %d", precision);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (precision != SQ_FP64) {
+        if (!D32 || !pairs->prim32 || !pairs->herm32 || (precision == SQ_FP32_BOYS32 && !table32))
+            return set_error(SQ_ERR_ARG, "sq_jk: FP32 precision needs D32, prim32, herm32 and table32");
+        rc = to_float((long long)basis->nbf * basis->nbf, D, D32, s);
+        if (rc) return rc;
+    }
+    EriArgs a{};
+    a.basis = *basis;
+    a.pairs = *pairs;
+    a.tab64 = table64;
+    a.tab32 = table32;
+    a.D = D;
+    a.D32 = D32;
+    a.Jacc = Jacc;
+    a.Kacc = Kacc;
+    return run_classes("sq_jk", a, quartets, MODE_JK, precision, s);
+}

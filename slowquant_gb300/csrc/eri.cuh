@@ -1,0 +1,423 @@
+// eri.cuh -- McMurchie-Davidson shell-quartet kernels, one template per
+// quartet class (LA LB | LC LD), one thread per contracted shell quartet.
+//
+// For every primitive quartet (bra pair ij, ket pair kl) the thread forms
+//   R_{tuv}(alpha, P-Q), t+u+v <= L,  scaled by 2 pi^{5/2} U_ij U_kl / sqrt(p+q)
+// (Boys function + the Hermite Coulomb recurrences of
+// slowquant/molecularintegrals/integralfunctions.py:100-148), contracts it with
+// the ket's Hermite coefficients into W[tuv][cd] (summed over ket primitive
+// pairs), and once per bra primitive pair contracts W with the bra's Hermite
+// coefficients into the contracted block (ab|cd).  This is the arithmetic of
+// electron_repulsion_integral (slowquant/molecularintegrals/electronrepulsion.py:
+// 107-297) reordered so that the contraction over ket primitives happens in
+// Hermite space; normalisation and contraction coefficients are folded into
+// the pair data.
+//
+// Epilogues: MODE_DENSE scatters the block to the eight index permutations of
+// a dense tensor (electronrepulsion.py:72-103); MODE_SCHWARZ stores
+// sqrt(max(block)) for diagonal quartets (electronrepulsion.py:300-339);
+// MODE_JK digests the block into Coulomb / exchange accumulators with the
+// 8-fold permutational weights (hartreefock_in_memory.py:55-56 without the
+// stored tensor).
+#pragma once
+
+#include <type_traits>
+
+#include "boys.cuh"
+#include "sq_common.cuh"
+
+namespace sq {
+
+enum { MODE_DENSE = 0, MODE_SCHWARZ = 1, MODE_JK = 2 };
+enum { BOYS_FP64 = 0, BOYS_FP32 = 1 };
+
+struct EriArgs {
+    sq_basis basis;
+    sq_pairs pairs;
+    const int2 *quartets;
+    long long nq;
+    const double *tab64;
+    const float *tab32;
+    const double *D;
+    const float *D32;
+    double *Jacc;
+    double *Kacc;
+    double *V;
+    double *q;
+};
+
+constexpr double kTwoPi52 = 34.98683665524972;  // 2 pi^{5/2}
+
+template <typename R>
+__device__ __forceinline__ const R *herm_ptr(const sq_pairs &pr) {
+    if constexpr (std::is_same<R, double>::value)
+        return pr.herm;
+    else
+        return pr.herm32;
+}
+template <typename R>
+__device__ __forceinline__ const R *prim_ptr(const sq_pairs &pr) {
+    if constexpr (std::is_same<R, double>::value)
+        return pr.prim;
+    else
+        return pr.prim32;
+}
+
+template <typename R>
+__device__ __forceinline__ R rsqrt_r(R x) {
+    if constexpr (std::is_same<R, double>::value)
+        return rsqrt(x);
+    else
+        return rsqrtf(x);
+}
+
+// Scaled R^{(0)}_{tuv} table for t+u+v <= L from Fs[n] = pref (-2 alpha)^n F_n.
+template <int L, typename R>
+__device__ __forceinline__ void hermite_r(const R (&Fs)[L + 1], R X, R Y, R Z, R (&out)[L + 1][L + 1][L + 1]) {
+    R cur[L + 1][L + 1][L + 1];
+    cur[0][0][0] = Fs[L];
+#pragma unroll
+    for (int n = L - 1; n >= 0; --n) {
+        R nxt[L + 1][L + 1][L + 1];
+        nxt[0][0][0] = Fs[n];
+        const int top = L - n;
+#pragma unroll
+        for (int t = 0; t <= top; ++t)
+#pragma unroll
+            for (int u = 0; u <= top - t; ++u)
+#pragma unroll
+                for (int v = 0; v <= top - t - u; ++v) {
+                    if (t + u + v == 0) continue;
+                    R val;
+                    if (t > 0) {
+                        val = X * cur[t - 1][u][v];
+                        if (t > 1) val = fma(R(t - 1), cur[t - 2][u][v], val);
+                    } else if (u > 0) {
+                        val = Y * cur[0][u - 1][v];
+                        if (u > 1) val = fma(R(u - 1), cur[0][u - 2][v], val);
+                    } else {
+                        val = Z * cur[0][0][v - 1];
+                        if (v > 1) val = fma(R(v - 1), cur[0][0][v - 2], val);
+                    }
+                    nxt[t][u][v] = val;
+                }
+#pragma unroll
+        for (int t = 0; t <= top; ++t)
+#pragma unroll
+            for (int u = 0; u <= top - t; ++u)
+#pragma unroll
+                for (int v = 0; v <= top - t - u; ++v) cur[t][u][v] = nxt[t][u][v];
+    }
+#pragma unroll
+    for (int t = 0; t <= L; ++t)
+#pragma unroll
+        for (int u = 0; u <= L - t; ++u)
+#pragma unroll
+            for (int v = 0; v <= L - t - u; ++v) out[t][u][v] = cur[t][u][v];
+}
+
+template <typename T>
+__device__ __forceinline__ T gload(const T *p) {
+    return __ldg(p);
+}
+
+// Contracted block of one quartet: acc[a*NB+b][c*ND+d].
+template <int LA, int LB, int LC, int LD, typename R, int BOYS>
+__device__ __forceinline__ void quartet_block(const EriArgs &args, int P, int Q,
+                                              R (&acc)[ncart(LA) * ncart(LB)][ncart(LC) * ncart(LD)]) {
+    constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
+    constexpr int NAB = NA * NB, NCD = NC * ND;
+    constexpr int LAB = LA + LB, LCD = LC + LD, L = LAB + LCD;
+    constexpr int EB = herm_size(LA, LB), EK = herm_size(LC, LD);
+
+    const sq_pairs &pr = args.pairs;
+    const R *prim = prim_ptr<R>(pr);
+    const R *herm = herm_ptr<R>(pr);
+    const int i0 = gload(pr.pp_off + P), i1 = gload(pr.pp_off + P + 1);
+    const int k0 = gload(pr.pp_off + Q), k1 = gload(pr.pp_off + Q + 1);
+    const R *hb = herm + gload(pr.herm_off + P);
+    const R *hk = herm + gload(pr.herm_off + Q);
+
+#pragma unroll
+    for (int x = 0; x < NAB; ++x)
+#pragma unroll
+        for (int y = 0; y < NCD; ++y) acc[x][y] = R(0);
+
+    for (int i = i0; i < i1; ++i) {
+        const R p = gload(prim + 8 * i + 0);
+        const R Px = gload(prim + 8 * i + 1), Py = gload(prim + 8 * i + 2), Pz = gload(prim + 8 * i + 3);
+        const R Ub = gload(prim + 8 * i + 4);
+        R W[LAB + 1][LAB + 1][LAB + 1][NCD];
+#pragma unroll
+        for (int t = 0; t <= LAB; ++t)
+#pragma unroll
+            for (int u = 0; u <= LAB - t; ++u)
+#pragma unroll
+                for (int v = 0; v <= LAB - t - u; ++v)
+#pragma unroll
+                    for (int y = 0; y < NCD; ++y) W[t][u][v][y] = R(0);
+
+        for (int k = k0; k < k1; ++k) {
+            const R q = gload(prim + 8 * k + 0);
+            const R X = Px - gload(prim + 8 * k + 1);
+            const R Y = Py - gload(prim + 8 * k + 2);
+            const R Z = Pz - gload(prim + 8 * k + 3);
+            const R Uk = gload(prim + 8 * k + 4);
+            const R r = rsqrt_r(p + q);
+            const R alpha = p * q * (r * r);
+            const R T = alpha * (X * X + Y * Y + Z * Z);
+            R Fs[L + 1];
+            if constexpr (std::is_same<R, double>::value) {
+                double F[L + 1];
+                boys64<L>(T, args.tab64, F);
+#pragma unroll
+                for (int n = 0; n <= L; ++n) Fs[n] = F[n];
+            } else if constexpr (BOYS == BOYS_FP64) {
+                double F[L + 1];
+                boys64<L>((double)T, args.tab64, F);
+#pragma unroll
+                for (int n = 0; n <= L; ++n) Fs[n] = (R)F[n];
+            } else {
+                float F[L + 1];
+                boys32<L>(T, args.tab32, F);
+#pragma unroll
+                for (int n = 0; n <= L; ++n) Fs[n] = F[n];
+            }
+            R fac = R(kTwoPi52) * Ub * Uk * r;
+            const R m2a = R(-2) * alpha;
+#pragma unroll
+            for (int n = 0; n <= L; ++n) {
+                Fs[n] *= fac;
+                fac *= m2a;
+            }
+            R Rt[L + 1][L + 1][L + 1];
+            hermite_r<L, R>(Fs, X, Y, Z, Rt);
+
+            // ket transform: W[tuv][cd] += sum_{tau nu phi} (-1)^{tau+nu+phi} E^{cd}_{tau nu phi} R[t+tau][u+nu][v+phi]
+            const R *ek = hk + (k - k0) * EK;
+#pragma unroll
+            for (int c = 0; c < NC; ++c)
+#pragma unroll
+                for (int d = 0; d < ND; ++d) {
+                    const int cx = cart_x(LC, c) + cart_x(LD, d);
+                    const int cy = cart_y(LC, c) + cart_y(LD, d);
+                    const int cz = cart_z(LC, c) + cart_z(LD, d);
+                    const int off = herm_offset(LC, LD, c, d);
+#pragma unroll
+                    for (int tau = 0; tau <= cx; ++tau)
+#pragma unroll
+                        for (int nu = 0; nu <= cy; ++nu)
+#pragma unroll
+                            for (int phi = 0; phi <= cz; ++phi) {
+                                R e = gload(ek + off + (tau * (cy + 1) + nu) * (cz + 1) + phi);
+                                if ((tau + nu + phi) & 1) e = -e;
+#pragma unroll
+                                for (int t = 0; t <= LAB; ++t)
+#pragma unroll
+                                    for (int u = 0; u <= LAB - t; ++u)
+#pragma unroll
+                                        for (int v = 0; v <= LAB - t - u; ++v)
+                                            W[t][u][v][c * ND + d] =
+                                                fma(e, Rt[t + tau][u + nu][v + phi], W[t][u][v][c * ND + d]);
+                            }
+                }
+        }
+        // bra transform
+        const R *eb = hb + (i - i0) * EB;
+#pragma unroll
+        for (int a = 0; a < NA; ++a)
+#pragma unroll
+            for (int b = 0; b < NB; ++b) {
+                const int ax = cart_x(LA, a) + cart_x(LB, b);
+                const int ay = cart_y(LA, a) + cart_y(LB, b);
+                const int az = cart_z(LA, a) + cart_z(LB, b);
+                const int off = herm_offset(LA, LB, a, b);
+#pragma unroll
+                for (int t = 0; t <= ax; ++t)
+#pragma unroll
+                    for (int u = 0; u <= ay; ++u)
+#pragma unroll
+                        for (int v = 0; v <= az; ++v) {
+                            const R e = gload(eb + off + (t * (ay + 1) + u) * (az + 1) + v);
+#pragma unroll
+                            for (int y = 0; y < NCD; ++y) acc[a * NB + b][y] = fma(e, W[t][u][v][y], acc[a * NB + b][y]);
+                        }
+            }
+    }
+}
+
+template <int LA, int LB, int LC, int LD, typename R, int BOYS, int MODE>
+__global__ void __launch_bounds__(128) eri_class_kernel(const EriArgs args) {
+    constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
+    constexpr int NAB = NA * NB, NCD = NC * ND;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long qi = (long long)blockIdx.x * blockDim.x + threadIdx.x; qi < args.nq; qi += stride) {
+        const int2 pq = args.quartets[qi];
+        const int P = pq.x, Q = pq.y;
+        R acc[NAB][NCD];
+        quartet_block<LA, LB, LC, LD, R, BOYS>(args, P, Q, acc);
+
+        const int sa = gload(args.pairs.shells + 2 * P), sb = gload(args.pairs.shells + 2 * P + 1);
+        const int sc = gload(args.pairs.shells + 2 * Q), sd = gload(args.pairs.shells + 2 * Q + 1);
+        const int oa = gload(args.basis.bf_off + sa), ob = gload(args.basis.bf_off + sb);
+        const int oc = gload(args.basis.bf_off + sc), od = gload(args.basis.bf_off + sd);
+        const long long n = args.basis.nbf;
+
+        if constexpr (MODE == MODE_SCHWARZ) {
+            R mx = acc[0][0];
+#pragma unroll
+            for (int x = 0; x < NAB; ++x)
+#pragma unroll
+                for (int y = 0; y < NCD; ++y) mx = acc[x][y] > mx ? acc[x][y] : mx;
+            args.q[P] = sqrt((double)mx);
+        } else if constexpr (MODE == MODE_DENSE) {
+            double *V = args.V;
+#pragma unroll
+            for (int a = 0; a < NA; ++a)
+#pragma unroll
+                for (int b = 0; b < NB; ++b)
+#pragma unroll
+                    for (int c = 0; c < NC; ++c)
+#pragma unroll
+                        for (int d = 0; d < ND; ++d) {
+                            const double v = acc[a * NB + b][c * ND + d];
+                            const long long A = oa + a, B = ob + b, C = oc + c, Dd = od + d;
+                            V[((A * n + B) * n + C) * n + Dd] = v;
+                            V[((B * n + A) * n + C) * n + Dd] = v;
+                            V[((A * n + B) * n + Dd) * n + C] = v;
+                            V[((B * n + A) * n + Dd) * n + C] = v;
+                            V[((C * n + Dd) * n + A) * n + B] = v;
+                            V[((Dd * n + C) * n + A) * n + B] = v;
+                            V[((C * n + Dd) * n + B) * n + A] = v;
+                            V[((Dd * n + C) * n + B) * n + A] = v;
+                        }
+        } else {
+            // Permutational weight m = 8 / 2^{[a==b] + [c==d] + [P==Q]}; J gets m/2, K gets m/4.
+            double m = 8.0;
+            if (sa == sb) m *= 0.5;
+            if (sc == sd) m *= 0.5;
+            if (P == Q) m *= 0.5;
+            const R wJ = R(0.5 * m), wK = R(0.25 * m);
+            const R *D;
+            if constexpr (std::is_same<R, double>::value)
+                D = args.D;
+            else
+                D = args.D32;
+            R Dab[NA][NB], Dcd[NC][ND], Dac[NA][NC], Dad[NA][ND], Dbc[NB][NC], Dbd[NB][ND];
+#pragma unroll
+            for (int a = 0; a < NA; ++a)
+#pragma unroll
+                for (int b = 0; b < NB; ++b) Dab[a][b] = gload(D + (oa + a) * n + ob + b);
+#pragma unroll
+            for (int c = 0; c < NC; ++c)
+#pragma unroll
+                for (int d = 0; d < ND; ++d) Dcd[c][d] = gload(D + (oc + c) * n + od + d);
+#pragma unroll
+            for (int a = 0; a < NA; ++a)
+#pragma unroll
+                for (int c = 0; c < NC; ++c) Dac[a][c] = gload(D + (oa + a) * n + oc + c);
+#pragma unroll
+            for (int a = 0; a < NA; ++a)
+#pragma unroll
+                for (int d = 0; d < ND; ++d) Dad[a][d] = gload(D + (oa + a) * n + od + d);
+#pragma unroll
+            for (int b = 0; b < NB; ++b)
+#pragma unroll
+                for (int c = 0; c < NC; ++c) Dbc[b][c] = gload(D + (ob + b) * n + oc + c);
+#pragma unroll
+            for (int b = 0; b < NB; ++b)
+#pragma unroll
+                for (int d = 0; d < ND; ++d) Dbd[b][d] = gload(D + (ob + b) * n + od + d);
+
+            R Jab[NA][NB], Jcd[NC][ND], Kac[NA][NC], Kad[NA][ND], Kbc[NB][NC], Kbd[NB][ND];
+#pragma unroll
+            for (int a = 0; a < NA; ++a)
+#pragma unroll
+                for (int b = 0; b < NB; ++b) Jab[a][b] = R(0);
+#pragma unroll
+            for (int c = 0; c < NC; ++c)
+#pragma unroll
+                for (int d = 0; d < ND; ++d) Jcd[c][d] = R(0);
+#pragma unroll
+            for (int a = 0; a < NA; ++a)
+#pragma unroll
+                for (int c = 0; c < NC; ++c) Kac[a][c] = R(0);
+#pragma unroll
+            for (int a = 0; a < NA; ++a)
+#pragma unroll
+                for (int d = 0; d < ND; ++d) Kad[a][d] = R(0);
+#pragma unroll
+            for (int b = 0; b < NB; ++b)
+#pragma unroll
+                for (int c = 0; c < NC; ++c) Kbc[b][c] = R(0);
+#pragma unroll
+            for (int b = 0; b < NB; ++b)
+#pragma unroll
+                for (int d = 0; d < ND; ++d) Kbd[b][d] = R(0);
+
+#pragma unroll
+            for (int a = 0; a < NA; ++a)
+#pragma unroll
+                for (int b = 0; b < NB; ++b)
+#pragma unroll
+                    for (int c = 0; c < NC; ++c)
+#pragma unroll
+                        for (int d = 0; d < ND; ++d) {
+                            const R v = acc[a * NB + b][c * ND + d];
+                            Jab[a][b] = fma(v, Dcd[c][d], Jab[a][b]);
+                            Jcd[c][d] = fma(v, Dab[a][b], Jcd[c][d]);
+                            Kac[a][c] = fma(v, Dbd[b][d], Kac[a][c]);
+                            Kbd[b][d] = fma(v, Dac[a][c], Kbd[b][d]);
+                            Kad[a][d] = fma(v, Dbc[b][c], Kad[a][d]);
+                            Kbc[b][c] = fma(v, Dad[a][d], Kbc[b][c]);
+                        }
+            double *J = args.Jacc, *K = args.Kacc;
+#pragma unroll
+            for (int a = 0; a < NA; ++a)
+#pragma unroll
+                for (int b = 0; b < NB; ++b) atomicAdd(J + (oa + a) * n + ob + b, (double)(wJ * Jab[a][b]));
+#pragma unroll
+            for (int c = 0; c < NC; ++c)
+#pragma unroll
+                for (int d = 0; d < ND; ++d) atomicAdd(J + (oc + c) * n + od + d, (double)(wJ * Jcd[c][d]));
+#pragma unroll
+            for (int a = 0; a < NA; ++a)
+#pragma unroll
+                for (int c = 0; c < NC; ++c) atomicAdd(K + (oa + a) * n + oc + c, (double)(wK * Kac[a][c]));
+#pragma unroll
+            for (int b = 0; b < NB; ++b)
+#pragma unroll
+                for (int d = 0; d < ND; ++d) atomicAdd(K + (ob + b) * n + od + d, (double)(wK * Kbd[b][d]));
+#pragma unroll
+            for (int a = 0; a < NA; ++a)
+#pragma unroll
+                for (int d = 0; d < ND; ++d) atomicAdd(K + (oa + a) * n + od + d, (double)(wK * Kad[a][d]));
+#pragma unroll
+            for (int b = 0; b < NB; ++b)
+#pragma unroll
+                for (int c = 0; c < NC; ++c) atomicAdd(K + (ob + b) * n + oc + c, (double)(wK * Kbc[b][c]));
+        }
+    }
+}
+
+// Host-side launcher table entry for one quartet class.
+typedef cudaError_t (*eri_launcher)(const EriArgs &args, int mode, int precision, cudaStream_t stream);
+
+template <int LA, int LB, int LC, int LD>
+cudaError_t launch_eri_class(const EriArgs &args, int mode, int precision, cudaStream_t stream) {
+    if (args.nq <= 0) return cudaSuccess;
+    const int threads = 128;
+    long long blocks = (args.nq + threads - 1) / threads;
+    const long long cap = 152LL * 16 * 8;
+    if (blocks > cap) blocks = cap;
+    (void)mode;  // per-thread kernels serve J/K launches only
+    if (precision == SQ_FP64)
+        eri_class_kernel<LA, LB, LC, LD, double, BOYS_FP64, MODE_JK><<<(int)blocks, threads, 0, stream>>>(args);
+    else if (precision == SQ_FP32)
+        eri_class_kernel<LA, LB, LC, LD, float, BOYS_FP64, MODE_JK><<<(int)blocks, threads, 0, stream>>>(args);
+    else
+        eri_class_kernel<LA, LB, LC, LD, float, BOYS_FP32, MODE_JK><<<(int)blocks, threads, 0, stream>>>(args);
+    return cudaGetLastError();
+}
+
+}  // namespace sq

@@ -1,0 +1,11 @@
+// eri_q10.cu -- per-thread J/K kernels of quartet class (dp|ss).
+// The dispatch table in capi.cu calls this launcher.
+#include "eri.cuh"
+
+namespace sq {
+
+cudaError_t launch_qc_10(const EriArgs &a, int mode, int prec, cudaStream_t s) {
+    return launch_eri_class<2, 1, 0, 0>(a, mode, prec, s);
+}
+
+}  // namespace sq

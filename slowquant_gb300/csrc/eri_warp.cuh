@@ -1,0 +1,367 @@
+// eri_warp.cuh -- generic warp-cooperative McMurchie-Davidson kernel for the
+// high angular-momentum quartet classes (L = la+lb+lc+ld >= 5).
+//
+// One warp owns one contracted shell quartet at a time.  Per primitive quartet:
+//   * lanes 0..L evaluate F_m(T) in parallel (one Taylor expansion each),
+//     scaled by pref (-2 alpha)^m;
+//   * the Hermite Coulomb recurrences (integralfunctions.py:100-148) run level
+//     by level, the entries of one level spread over the lanes, in a
+//     warp-private shared-memory buffer;
+//   * the ket transform W[h][cd] += sum (-1)^{tau+nu+phi} E^{cd}_{tau nu phi}
+//     R[h + (tau,nu,phi)] is spread over lanes by output entry (cd-major).
+// After the ket primitive loop the bra transform (ab|cd) += sum_h E^{ab}_h W[h][cd]
+// runs with lanes owning output entries, accumulated in registers.  The
+// arithmetic is that of the per-thread kernel (eri.cuh); the class is a
+// runtime parameter, so one compiled kernel serves every class.
+#pragma once
+
+#include "boys.cuh"
+#include "eri.cuh"
+
+namespace sq {
+
+constexpr int kWarpHmax = nherm(2 * SQ_LMAX * 2);          // Hermite table for L <= 4*lmax
+constexpr int kWarpWmax = nherm(2 * SQ_LMAX) * ncart(SQ_LMAX) * ncart(SQ_LMAX);  // W entries
+constexpr int kWarpAccMax = (ncart(SQ_LMAX) * ncart(SQ_LMAX) * ncart(SQ_LMAX) * ncart(SQ_LMAX) + 31) / 32;
+constexpr int kWarpsPerBlock = 4;
+
+struct WarpClass {
+    int la, lb, lc, ld;
+};
+
+// Flat Hermite index: degree n = t+u+v ascending, then t descending, then u descending.
+__host__ __device__ __forceinline__ int herm_index(int t, int u, int v) {
+    const int n = t + u + v;
+    return n * (n + 1) * (n + 2) / 6 + (n - t) * (n - t + 1) / 2 + (n - t - u);
+}
+
+template <typename R>
+struct WarpSmem {
+    R rbuf[2][kWarpHmax];
+    R W[kWarpWmax];
+    R Fs[16];
+};
+
+__device__ __forceinline__ void cart_powers(int l, int c, int &x, int &y, int &z) {
+    int idx = 0;
+    for (int xx = l; xx >= 0; --xx)
+        for (int yy = l - xx; yy >= 0; --yy) {
+            if (idx == c) {
+                x = xx;
+                y = yy;
+                z = l - xx - yy;
+                return;
+            }
+            ++idx;
+        }
+    x = y = z = 0;
+}
+
+__device__ __forceinline__ int herm_offset_rt(int la, int lb, int a, int b) {
+    const int nb = ncart(lb);
+    int off = 0;
+    for (int aa = 0; aa < ncart(la); ++aa) {
+        int ax, ay, az;
+        cart_powers(la, aa, ax, ay, az);
+        for (int bb = 0; bb < nb; ++bb) {
+            if (aa == a && bb == b) return off;
+            int bx, by, bz;
+            cart_powers(lb, bb, bx, by, bz);
+            off += (ax + bx + 1) * (ay + by + 1) * (az + bz + 1);
+        }
+    }
+    return off;
+}
+
+template <typename R, int BOYS, int MODE>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const EriArgs args, const WarpClass cls) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    WarpSmem<R> &sm = reinterpret_cast<WarpSmem<R> *>(smem_raw)[warp];
+    // per-block tables: (t,u,v) of each flat Hermite index; E offsets of component pairs
+    __shared__ int s_tuv[kWarpHmax];
+    __shared__ short s_hoff_b[ncart(SQ_LMAX) * ncart(SQ_LMAX)];
+    __shared__ short s_hoff_k[ncart(SQ_LMAX) * ncart(SQ_LMAX)];
+    __shared__ int s_pw_b[ncart(SQ_LMAX) * ncart(SQ_LMAX)];  // packed (ax+bx, ay+by, az+bz)
+    __shared__ int s_pw_k[ncart(SQ_LMAX) * ncart(SQ_LMAX)];
+
+    const int la = cls.la, lb = cls.lb, lc = cls.lc, ld = cls.ld;
+    const int NA = ncart(la), NB = ncart(lb), NC = ncart(lc), ND = ncart(ld);
+    const int NAB = NA * NB, NCD = NC * ND;
+    const int LAB = la + lb, L = LAB + lc + ld;
+    const int HAB = nherm(LAB), HL = nherm(L);
+    const int EB = herm_offset_rt(la, lb, NA, 0), EK = herm_offset_rt(lc, ld, NC, 0);
+    const int NW = HAB * NCD, NACC = NAB * NCD;
+
+    for (int e = threadIdx.x; e < HL; e += blockDim.x) {
+        // invert herm_index
+        int n = 0;
+        while ((n + 1) * (n + 2) * (n + 3) / 6 <= e) ++n;
+        int r = e - n * (n + 1) * (n + 2) / 6;
+        int t = n;
+        while (r >= n - t + 1) {
+            r -= n - t + 1;
+            --t;
+        }
+        const int u = n - t - r, v = n - t - u;
+        s_tuv[e] = t | (u << 8) | (v << 16);
+    }
+    for (int x = threadIdx.x; x < NAB; x += blockDim.x) {
+        const int a = x / NB, b = x % NB;
+        s_hoff_b[x] = (short)herm_offset_rt(la, lb, a, b);
+        int ax, ay, az, bx, by, bz;
+        cart_powers(la, a, ax, ay, az);
+        cart_powers(lb, b, bx, by, bz);
+        s_pw_b[x] = (ax + bx) | ((ay + by) << 8) | ((az + bz) << 16);
+    }
+    for (int x = threadIdx.x; x < NCD; x += blockDim.x) {
+        const int c = x / ND, d = x % ND;
+        s_hoff_k[x] = (short)herm_offset_rt(lc, ld, c, d);
+        int cx, cy, cz, dx, dy, dz;
+        cart_powers(lc, c, cx, cy, cz);
+        cart_powers(ld, d, dx, dy, dz);
+        s_pw_k[x] = (cx + dx) | ((cy + dy) << 8) | ((cz + dz) << 16);
+    }
+    __syncthreads();
+
+    const sq_pairs &pr = args.pairs;
+    const R *prim = prim_ptr<R>(pr);
+    const R *herm = herm_ptr<R>(pr);
+    const long long nwarps = (long long)gridDim.x * kWarpsPerBlock;
+    const int kacc = (NACC + 31) >> 5;
+
+    for (long long qi = (long long)blockIdx.x * kWarpsPerBlock + warp; qi < args.nq; qi += nwarps) {
+        const int2 pq = args.quartets[qi];
+        const int P = pq.x, Q = pq.y;
+        const int i0 = gload(pr.pp_off + P), i1 = gload(pr.pp_off + P + 1);
+        const int k0 = gload(pr.pp_off + Q), k1 = gload(pr.pp_off + Q + 1);
+        const R *hb = herm + gload(pr.herm_off + P);
+        const R *hk = herm + gload(pr.herm_off + Q);
+        R acc[kWarpAccMax];
+#pragma unroll
+        for (int k = 0; k < kWarpAccMax; ++k) acc[k] = R(0);
+
+        for (int i = i0; i < i1; ++i) {
+            const R p = gload(prim + 8 * i + 0);
+            const R Px = gload(prim + 8 * i + 1), Py = gload(prim + 8 * i + 2), Pz = gload(prim + 8 * i + 3);
+            const R Ub = gload(prim + 8 * i + 4);
+            for (int w = lane; w < NW; w += 32) sm.W[w] = R(0);
+            for (int k = k0; k < k1; ++k) {
+                const R q = gload(prim + 8 * k + 0);
+                const R X = Px - gload(prim + 8 * k + 1);
+                const R Y = Py - gload(prim + 8 * k + 2);
+                const R Z = Pz - gload(prim + 8 * k + 3);
+                const R Uk = gload(prim + 8 * k + 4);
+                const R r = rsqrt_r(p + q);
+                const R alpha = p * q * (r * r);
+                const R T = alpha * (X * X + Y * Y + Z * Z);
+                // lane m <= L: Fs[m] = pref (-2 alpha)^m F_m(T)
+                if (lane <= L) {
+                    R Fm;
+                    const int m = lane;
+                    if constexpr (std::is_same<R, double>::value || BOYS == BOYS_FP64) {
+                        const double Td = (double)T;
+                        double f;
+                        if (Td < SQ_BOYS_TMAX) {
+                            const int kk = __double2int_rn(Td * SQ_BOYS_STEP_INV);
+                            const double dd = Td - kk * (1.0 / SQ_BOYS_STEP_INV);
+                            const double *row = args.tab64 + kk * SQ_BOYS_NCOL + m;
+                            f = __ldg(row + kBoysTaylor64 - 1);
+#pragma unroll
+                            for (int j = kBoysTaylor64 - 1; j >= 1; --j) f = fma(f, -dd * (1.0 / j), __ldg(row + j - 1));
+                        } else {
+                            const double rr = rsqrt(Td);
+                            f = kSqrtPiHalf * rr;
+                            const double h = 0.5 * rr * rr;
+                            for (int j = 0; j < m; ++j) f *= (2 * j + 1) * h;
+                        }
+                        Fm = (R)f;
+                    } else {
+                        float f;
+                        if (T < (float)SQ_BOYS_TMAX) {
+                            const int kk = __float2int_rn(T * (float)SQ_BOYS_STEP_INV);
+                            const float dd = T - kk * (1.0f / SQ_BOYS_STEP_INV);
+                            const float *row = args.tab32 + kk * SQ_BOYS_NCOL + m;
+                            f = __ldg(row + kBoysTaylor32 - 1);
+#pragma unroll
+                            for (int j = kBoysTaylor32 - 1; j >= 1; --j) f = fmaf(f, -dd * (1.0f / j), __ldg(row + j - 1));
+                        } else {
+                            const float rr = rsqrtf(T);
+                            f = (float)kSqrtPiHalf * rr;
+                            const float h = 0.5f * rr * rr;
+                            for (int j = 0; j < m; ++j) f *= (2 * j + 1) * h;
+                        }
+                        Fm = f;
+                    }
+                    // pref (-2 alpha)^m
+                    R fac = R(kTwoPi52) * Ub * Uk * r;
+                    const R m2a = R(-2) * alpha;
+                    for (int j = 0; j < m; ++j) fac *= m2a;
+                    sm.Fs[m] = Fm * fac;
+                }
+                __syncwarp();
+                // Hermite recurrences, level L (top) down to 0
+                R *cur = sm.rbuf[0], *nxt = sm.rbuf[1];
+                if (lane == 0) cur[0] = sm.Fs[L];
+                __syncwarp();
+                for (int n = L - 1; n >= 0; --n) {
+                    const int cnt = nherm(L - n);
+                    for (int e = lane; e < cnt; e += 32) {
+                        R val;
+                        if (e == 0) {
+                            val = sm.Fs[n];
+                        } else {
+                            const int tuv = s_tuv[e];
+                            const int t = tuv & 255, u = (tuv >> 8) & 255, v = tuv >> 16;
+                            if (t > 0) {
+                                val = X * cur[herm_index(t - 1, u, v)];
+                                if (t > 1) val = fma(R(t - 1), cur[herm_index(t - 2, u, v)], val);
+                            } else if (u > 0) {
+                                val = Y * cur[herm_index(0, u - 1, v)];
+                                if (u > 1) val = fma(R(u - 1), cur[herm_index(0, u - 2, v)], val);
+                            } else {
+                                val = Z * cur[herm_index(0, 0, v - 1)];
+                                if (v > 1) val = fma(R(v - 1), cur[herm_index(0, 0, v - 2)], val);
+                            }
+                        }
+                        nxt[e] = val;
+                    }
+                    __syncwarp();
+                    R *tmp = cur;
+                    cur = nxt;
+                    nxt = tmp;
+                }
+                // ket transform
+                const R *ek = hk + (long long)(k - k0) * EK;
+                for (int w = lane; w < NW; w += 32) {
+                    const int cd = w / HAB, h = w - cd * HAB;
+                    const int tuv = s_tuv[h];
+                    const int t = tuv & 255, u = (tuv >> 8) & 255, v = tuv >> 16;
+                    const int pw = s_pw_k[cd];
+                    const int cx = pw & 255, cy = (pw >> 8) & 255, cz = pw >> 16;
+                    const R *e = ek + s_hoff_k[cd];
+                    R s = R(0);
+                    for (int tau = 0; tau <= cx; ++tau)
+                        for (int nu = 0; nu <= cy; ++nu)
+                            for (int phi = 0; phi <= cz; ++phi) {
+                                R ev = gload(e + (tau * (cy + 1) + nu) * (cz + 1) + phi);
+                                if ((tau + nu + phi) & 1) ev = -ev;
+                                s = fma(ev, cur[herm_index(t + tau, u + nu, v + phi)], s);
+                            }
+                    sm.W[w] += s;
+                }
+                __syncwarp();
+            }
+            // bra transform: lanes own output entries x = lane + 32 kk, x = ab * NCD + cd
+            const R *eb = hb + (long long)(i - i0) * EB;
+#pragma unroll
+            for (int kk = 0; kk < kWarpAccMax; ++kk) {
+                if (kk < kacc) {
+                    const int x = lane + 32 * kk;
+                    if (x < NACC) {
+                        const int ab = x / NCD, cd = x - ab * NCD;
+                        const int pw = s_pw_b[ab];
+                        const int ax = pw & 255, ay = (pw >> 8) & 255, az = pw >> 16;
+                        const R *e = eb + s_hoff_b[ab];
+                        R s = R(0);
+                        for (int t = 0; t <= ax; ++t)
+                            for (int u = 0; u <= ay; ++u)
+                                for (int v = 0; v <= az; ++v)
+                                    s = fma(gload(e + (t * (ay + 1) + u) * (az + 1) + v), sm.W[herm_index(t, u, v) + HAB * cd], s);
+                        acc[kk] += s;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+
+        // epilogue
+        const int sa = gload(pr.shells + 2 * P), sb = gload(pr.shells + 2 * P + 1);
+        const int sc = gload(pr.shells + 2 * Q), sd = gload(pr.shells + 2 * Q + 1);
+        const long long n = args.basis.nbf;
+        const int oa = gload(args.basis.bf_off + sa), ob = gload(args.basis.bf_off + sb);
+        const int oc = gload(args.basis.bf_off + sc), od = gload(args.basis.bf_off + sd);
+        if constexpr (MODE == MODE_SCHWARZ) {
+            double mx = -1e300;
+#pragma unroll
+            for (int kk = 0; kk < kWarpAccMax; ++kk)
+                if (kk < kacc && lane + 32 * kk < NACC) mx = fmax(mx, (double)acc[kk]);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+            if (lane == 0) args.q[P] = sqrt(mx);
+        } else {
+            double m = 8.0;
+            if (sa == sb) m *= 0.5;
+            if (sc == sd) m *= 0.5;
+            if (P == Q) m *= 0.5;
+#pragma unroll
+            for (int kk = 0; kk < kWarpAccMax; ++kk) {
+                if (kk < kacc) {
+                    const int x = lane + 32 * kk;
+                    if (x < NACC) {
+                        const int ab = x / NCD, cd = x - ab * NCD;
+                        const long long A = oa + ab / NB, B = ob + ab % NB, C = oc + cd / ND, Dd = od + cd % ND;
+                        const double v = (double)acc[kk];
+                        if constexpr (MODE == MODE_DENSE) {
+                            double *V = args.V;
+                            V[((A * n + B) * n + C) * n + Dd] = v;
+                            V[((B * n + A) * n + C) * n + Dd] = v;
+                            V[((A * n + B) * n + Dd) * n + C] = v;
+                            V[((B * n + A) * n + Dd) * n + C] = v;
+                            V[((C * n + Dd) * n + A) * n + B] = v;
+                            V[((Dd * n + C) * n + A) * n + B] = v;
+                            V[((C * n + Dd) * n + B) * n + A] = v;
+                            V[((Dd * n + C) * n + B) * n + A] = v;
+                        } else {
+                            const double *D = args.D;
+                            const double wJ = 0.5 * m * v, wK = 0.25 * m * v;
+                            double *J = args.Jacc, *K = args.Kacc;
+                            atomicAdd(J + A * n + B, wJ * gload(D + C * n + Dd));
+                            atomicAdd(J + C * n + Dd, wJ * gload(D + A * n + B));
+                            atomicAdd(K + A * n + C, wK * gload(D + B * n + Dd));
+                            atomicAdd(K + B * n + Dd, wK * gload(D + A * n + C));
+                            atomicAdd(K + A * n + Dd, wK * gload(D + B * n + C));
+                            atomicAdd(K + B * n + C, wK * gload(D + A * n + Dd));
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <typename R>
+constexpr size_t warp_smem_bytes() {
+    return sizeof(WarpSmem<R>) * kWarpsPerBlock;
+}
+
+inline cudaError_t launch_eri_warp(const EriArgs &args, const WarpClass &cls, int mode, int precision,
+                                   cudaStream_t stream) {
+    if (args.nq <= 0) return cudaSuccess;
+    long long blocks = (args.nq + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    const long long cap = 152LL * 64;
+    if (blocks > cap) blocks = cap;
+    const dim3 grid((unsigned)blocks), block(32 * kWarpsPerBlock);
+#define SQ_WARP_LAUNCH(R, B, M)                                                                                 \
+    do {                                                                                                        \
+        auto kern = eri_warp_kernel<R, B, M>;                                                                   \
+        const size_t sz = warp_smem_bytes<R>();                                                                 \
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sz);       \
+        if (e != cudaSuccess) return e;                                                                         \
+        kern<<<grid, block, sz, stream>>>(args, cls);                                                           \
+    } while (0)
+    if (mode == MODE_DENSE)
+        SQ_WARP_LAUNCH(double, BOYS_FP64, MODE_DENSE);
+    else if (mode == MODE_SCHWARZ)
+        SQ_WARP_LAUNCH(double, BOYS_FP64, MODE_SCHWARZ);
+    else if (precision == SQ_FP64)
+        SQ_WARP_LAUNCH(double, BOYS_FP64, MODE_JK);
+    else if (precision == SQ_FP32)
+        SQ_WARP_LAUNCH(float, BOYS_FP64, MODE_JK);
+    else
+        SQ_WARP_LAUNCH(float, BOYS_FP32, MODE_JK);
+#undef SQ_WARP_LAUNCH
+    return cudaGetLastError();
+}
+
+}  // namespace sq

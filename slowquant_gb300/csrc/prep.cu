@@ -1,0 +1,423 @@
+// prep.cu -- Boys grid, primitive-pair data, one-electron matrices and the
+// small utility kernels (quartet-list expansion, Fock assembly).
+#include <cstdio>
+
+#include "boys.cuh"
+#include "capi_internal.cuh"
+#include "sq_common.cuh"
+
+namespace sq {
+
+// ---------------------------------------------------------------------------
+// Boys grid: one thread per (grid point, order); compensated series sum.
+__global__ void boys_table_kernel(double *tab64, float *tab32) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= SQ_BOYS_NGRID * SQ_BOYS_NCOL) return;
+    const int k = idx / SQ_BOYS_NCOL, m = idx % SQ_BOYS_NCOL;
+    const double T = k * (1.0 / SQ_BOYS_STEP_INV);
+    double val;
+    if (m == SQ_BOYS_NCOL - 1) {
+        val = exp(-T);
+    } else {
+        // F_m(T) = e^{-T} sum_i (2T)^i / ((2m+1)(2m+3)...(2m+2i+1))
+        double term = 1.0 / (2 * m + 1), sum = 0.0, comp = 0.0;
+        for (int i = 0; i < 400; ++i) {
+            const double y = term - comp;
+            const double t = sum + y;
+            comp = (t - sum) - y;
+            sum = t;
+            term *= (2.0 * T) / (2 * m + 2 * i + 3);
+            if (term < 1e-18 * sum) break;
+        }
+        val = sum * exp(-T);
+    }
+    tab64[idx] = val;
+    if (tab32) tab32[idx] = (float)val;
+}
+
+__global__ void boys_eval_kernel(int n_max, const double *z, long long nz, const double *tab, double *out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nz) return;
+    double F[SQ_BOYS_NCOL];
+    boys64_rt(n_max, z[i], tab, F);
+    for (int m = 0; m <= n_max; ++m) out[i * (n_max + 1) + m] = F[m];
+}
+
+// ---------------------------------------------------------------------------
+// Primitive-pair data.  One thread per primitive pair.
+// 1D MD expansion coefficients E^{ij}_t / E^{00}_0 per Cartesian direction
+// (integralfunctions.py:9-71; the common factor exp(-mu X_AB^2) of all three
+// directions is kept in U).
+constexpr int kEMax = 4;  // supports l <= 3 per shell
+__device__ inline void ecoef_1d(double XPA, double XPB, double inv2p, int la, int lb,
+                                double (&E)[kEMax][kEMax][2 * kEMax - 1]) {
+    for (int i = 0; i <= la; ++i)
+        for (int j = 0; j <= lb; ++j)
+            for (int t = 0; t <= la + lb; ++t) E[i][j][t] = 0.0;
+    E[0][0][0] = 1.0;
+    for (int i = 0; i <= la; ++i)
+        for (int j = 0; j <= lb; ++j) {
+            if (i == 0 && j == 0) continue;
+            for (int t = 0; t <= i + j; ++t) {
+                double v = 0.0;
+                if (i == 0) {  // increment j
+                    if (t > 0) v += inv2p * E[0][j - 1][t - 1];
+                    if (t <= i + j - 1) v += XPB * E[0][j - 1][t];
+                    if (t + 1 <= i + j - 1) v += (t + 1) * E[0][j - 1][t + 1];
+                } else {  // increment i
+                    if (t > 0) v += inv2p * E[i - 1][j][t - 1];
+                    if (t <= i + j - 1) v += XPA * E[i - 1][j][t];
+                    if (t + 1 <= i + j - 1) v += (t + 1) * E[i - 1][j][t + 1];
+                }
+                E[i][j][t] = v;
+            }
+        }
+}
+
+__device__ inline double comp_norm(int l, int c) {
+    return 1.0 / sqrt(dfact_odd(cart_x(l, c)) * dfact_odd(cart_y(l, c)) * dfact_odd(cart_z(l, c)));
+}
+
+__global__ void pair_prep_kernel(const sq_basis basis, sq_pairs pairs) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= pairs.nprimpair) return;
+    // pair owning this primitive pair: largest P with pp_off[P] <= idx
+    int lo = 0, hi = pairs.npair - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pairs.pp_off[mid] <= idx) lo = mid;
+        else hi = mid - 1;
+    }
+    const int P = lo;
+    const int a = pairs.shells[2 * P], b = pairs.shells[2 * P + 1];
+    const int la = basis.l[a], lb = basis.l[b];
+    const int local = idx - pairs.pp_off[P];
+    const int nbp = basis.nprim[b];
+    const int ia = local / nbp, ib = local % nbp;
+    const double al = basis.exps[basis.prim_off[a] + ia], be = basis.exps[basis.prim_off[b] + ib];
+    const double ca = basis.coefs[basis.prim_off[a] + ia], cb = basis.coefs[basis.prim_off[b] + ib];
+    const double *A = basis.center + 3 * a, *B = basis.center + 3 * b;
+    const double p = al + be, mu = al * be / p;
+    double Pc[3], AB2 = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        Pc[d] = (al * A[d] + be * B[d]) / p;
+        AB2 += (A[d] - B[d]) * (A[d] - B[d]);
+    }
+    const double U = ca * cb * exp(-mu * AB2) / p;
+    double *pd = pairs.prim + 8 * (long long)idx;
+    pd[0] = p;
+    pd[1] = Pc[0];
+    pd[2] = Pc[1];
+    pd[3] = Pc[2];
+    pd[4] = U;
+    pd[5] = pd[6] = pd[7] = 0.0;
+    if (pairs.prim32) {
+        float *pf = pairs.prim32 + 8 * (long long)idx;
+        for (int x = 0; x < 8; ++x) pf[x] = (float)pd[x];
+    }
+    double E[3][kEMax][kEMax][2 * kEMax - 1];
+    for (int d = 0; d < 3; ++d) ecoef_1d(Pc[d] - A[d], Pc[d] - B[d], 0.5 / p, la, lb, E[d]);
+    const int na = ncart(la), nb = ncart(lb);
+    int esize = 0;
+    for (int x = 0; x < na; ++x)
+        for (int y = 0; y < nb; ++y) esize += herm_terms(la, x, lb, y);
+    const long long base = pairs.herm_off[P] + (long long)local * esize;
+    long long o = base;
+    for (int x = 0; x < na; ++x) {
+        const int ax = cart_x(la, x), ay = cart_y(la, x), az = cart_z(la, x);
+        const double sa = comp_norm(la, x);
+        for (int y = 0; y < nb; ++y) {
+            const int bx = cart_x(lb, y), by = cart_y(lb, y), bz = cart_z(lb, y);
+            const double s = sa * comp_norm(lb, y);
+            for (int t = 0; t <= ax + bx; ++t)
+                for (int u = 0; u <= ay + by; ++u)
+                    for (int v = 0; v <= az + bz; ++v) {
+                        const double e = s * E[0][ax][bx][t] * E[1][ay][by][u] * E[2][az][bz][v];
+                        pairs.herm[o] = e;
+                        if (pairs.herm32) pairs.herm32[o] = (float)e;
+                        ++o;
+                    }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// One-electron matrices; one thread per shell pair (s1 >= s2).
+constexpr int kE1 = 6;  // l+2 <= 5 (f shells + 2)
+
+__device__ inline void ecoef_1d_big(double XPA, double XPB, double inv2p, int la, int lb,
+                                    double (&E)[kE1][kE1][2 * kE1 - 1]) {
+    for (int i = 0; i <= la; ++i)
+        for (int j = 0; j <= lb; ++j)
+            for (int t = 0; t <= la + lb; ++t) E[i][j][t] = 0.0;
+    E[0][0][0] = 1.0;
+    for (int i = 0; i <= la; ++i)
+        for (int j = 0; j <= lb; ++j) {
+            if (i == 0 && j == 0) continue;
+            for (int t = 0; t <= i + j; ++t) {
+                double v = 0.0;
+                if (i == 0) {
+                    if (t > 0) v += inv2p * E[0][j - 1][t - 1];
+                    if (t <= i + j - 1) v += XPB * E[0][j - 1][t];
+                    if (t + 1 <= i + j - 1) v += (t + 1) * E[0][j - 1][t + 1];
+                } else {
+                    if (t > 0) v += inv2p * E[i - 1][j][t - 1];
+                    if (t <= i + j - 1) v += XPA * E[i - 1][j][t];
+                    if (t + 1 <= i + j - 1) v += (t + 1) * E[i - 1][j][t + 1];
+                }
+                E[i][j][t] = v;
+            }
+        }
+}
+
+// R^0_{tuv}, t+u+v <= L (L <= 6), flat index ((t*7)+u)*7+v.
+__device__ inline void hermite_r_rt(int L, double p, const double *PC, const double *tab, double *out) {
+    double F[SQ_BOYS_NCOL];
+    const double T = p * (PC[0] * PC[0] + PC[1] * PC[1] + PC[2] * PC[2]);
+    boys64_rt(L, T, tab, F);
+    double cur[343], nxt[343];
+#define RI(t, u, v) (((t) * 7 + (u)) * 7 + (v))
+    double fac = 1.0;
+    for (int n = 0; n <= L; ++n) {
+        F[n] *= fac;
+        fac *= -2.0 * p;
+    }
+    cur[0] = F[L];
+    for (int n = L - 1; n >= 0; --n) {
+        const int top = L - n;
+        nxt[0] = F[n];
+        for (int t = 0; t <= top; ++t)
+            for (int u = 0; u <= top - t; ++u)
+                for (int v = 0; v <= top - t - u; ++v) {
+                    if (t + u + v == 0) continue;
+                    double val;
+                    if (t > 0) {
+                        val = PC[0] * cur[RI(t - 1, u, v)];
+                        if (t > 1) val += (t - 1) * cur[RI(t - 2, u, v)];
+                    } else if (u > 0) {
+                        val = PC[1] * cur[RI(0, u - 1, v)];
+                        if (u > 1) val += (u - 1) * cur[RI(0, u - 2, v)];
+                    } else {
+                        val = PC[2] * cur[RI(0, 0, v - 1)];
+                        if (v > 1) val += (v - 1) * cur[RI(0, 0, v - 2)];
+                    }
+                    nxt[RI(t, u, v)] = val;
+                }
+        for (int t = 0; t <= top; ++t)
+            for (int u = 0; u <= top - t; ++u)
+                for (int v = 0; v <= top - t - u; ++v) cur[RI(t, u, v)] = nxt[RI(t, u, v)];
+    }
+    for (int t = 0; t <= L; ++t)
+        for (int u = 0; u <= L - t; ++u)
+            for (int v = 0; v <= L - t - u; ++v) out[RI(t, u, v)] = cur[RI(t, u, v)];
+#undef RI
+}
+
+__global__ void one_electron_kernel(const sq_basis basis, const double *tab, double *S, double *Tm, double *Vm) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ns = basis.nshell;
+    if (idx >= ns * (ns + 1) / 2) return;
+    // idx -> (s1, s2), s1 >= s2
+    int s1 = (int)((sqrt(8.0 * idx + 1.0) - 1.0) * 0.5);
+    while ((s1 + 1) * (s1 + 2) / 2 <= idx) ++s1;
+    while (s1 * (s1 + 1) / 2 > idx) --s1;
+    const int s2 = idx - s1 * (s1 + 1) / 2;
+    const int l1 = basis.l[s1], l2 = basis.l[s2];
+    const int n1 = ncart(l1), n2 = ncart(l2);
+    const int np1 = basis.nprim[s1], np2 = basis.nprim[s2];
+    const double *A = basis.center + 3 * s1, *B = basis.center + 3 * s2;
+    double sblk[100], tblk[100], vblk[100];
+    for (int x = 0; x < n1 * n2; ++x) sblk[x] = tblk[x] = vblk[x] = 0.0;
+    double E[3][kE1][kE1][2 * kE1 - 1];
+    double R[343];
+    constexpr double pi = 3.141592653589793;
+    for (int i = 0; i < np1; ++i)
+        for (int j = 0; j < np2; ++j) {
+            const double al = basis.exps[basis.prim_off[s1] + i], be = basis.exps[basis.prim_off[s2] + j];
+            const double cc = basis.coefs[basis.prim_off[s1] + i] * basis.coefs[basis.prim_off[s2] + j];
+            const double p = al + be, mu = al * be / p;
+            double Pc[3], AB2 = 0.0;
+            for (int d = 0; d < 3; ++d) {
+                Pc[d] = (al * A[d] + be * B[d]) / p;
+                AB2 += (A[d] - B[d]) * (A[d] - B[d]);
+            }
+            const double K = exp(-mu * AB2);
+            for (int d = 0; d < 3; ++d) ecoef_1d_big(Pc[d] - A[d], Pc[d] - B[d], 0.5 / p, l1 + 2, l2, E[d]);
+            const double sp = pi / p;
+            const double ov = sp * sqrt(sp);
+            for (int x = 0; x < n1; ++x) {
+                const int a[3] = {cart_x(l1, x), cart_y(l1, x), cart_z(l1, x)};
+                const double na = comp_norm(l1, x);
+                for (int y = 0; y < n2; ++y) {
+                    const int b[3] = {cart_x(l2, y), cart_y(l2, y), cart_z(l2, y)};
+                    const double w = cc * K * na * comp_norm(l2, y);
+                    double e0[3], d2[3];
+                    for (int d = 0; d < 3; ++d) {
+                        e0[d] = E[d][a[d]][b[d]][0];
+                        d2[d] = 4 * al * al * E[d][a[d] + 2][b[d]][0] - 2 * al * (2 * a[d] + 1) * e0[d] +
+                                (a[d] >= 2 ? a[d] * (a[d] - 1) * E[d][a[d] - 2][b[d]][0] : 0.0);
+                    }
+                    sblk[x * n2 + y] += w * ov * e0[0] * e0[1] * e0[2];
+                    tblk[x * n2 + y] += w * (-0.5 * ov) *
+                                        (d2[0] * e0[1] * e0[2] + e0[0] * d2[1] * e0[2] + e0[0] * e0[1] * d2[2]);
+                }
+            }
+            if (Vm) {
+                const int L = l1 + l2;
+                for (int at = 0; at < basis.natom; ++at) {
+                    double PC[3];
+                    for (int d = 0; d < 3; ++d) PC[d] = Pc[d] - basis.atom_xyz[3 * at + d];
+                    hermite_r_rt(L, p, PC, tab, R);
+                    const double zf = -2.0 * pi / p * basis.atom_charge[at];
+                    for (int x = 0; x < n1; ++x) {
+                        const int a[3] = {cart_x(l1, x), cart_y(l1, x), cart_z(l1, x)};
+                        const double na = comp_norm(l1, x);
+                        for (int y = 0; y < n2; ++y) {
+                            const int b[3] = {cart_x(l2, y), cart_y(l2, y), cart_z(l2, y)};
+                            double acc = 0.0;
+                            for (int t = 0; t <= a[0] + b[0]; ++t)
+                                for (int u = 0; u <= a[1] + b[1]; ++u)
+                                    for (int v = 0; v <= a[2] + b[2]; ++v)
+                                        acc += E[0][a[0]][b[0]][t] * E[1][a[1]][b[1]][u] * E[2][a[2]][b[2]][v] *
+                                               R[(t * 7 + u) * 7 + v];
+                            vblk[x * n2 + y] += cc * K * na * comp_norm(l2, y) * zf * acc;
+                        }
+                    }
+                }
+            }
+        }
+    const long long n = basis.nbf;
+    const int o1 = basis.bf_off[s1], o2 = basis.bf_off[s2];
+    for (int x = 0; x < n1; ++x)
+        for (int y = 0; y < n2; ++y) {
+            const long long r = o1 + x, c = o2 + y;
+            if (S) S[r * n + c] = S[c * n + r] = sblk[x * n2 + y];
+            if (Tm) Tm[r * n + c] = Tm[c * n + r] = tblk[x * n2 + y];
+            if (Vm) Vm[r * n + c] = Vm[c * n + r] = vblk[x * n2 + y];
+        }
+}
+
+// ---------------------------------------------------------------------------
+__global__ void quartets_expand_kernel(long long ntask, const int *bra, const int *ket_start, const int *count,
+                                       const long long *offset, const int *ket_list, int2 *out, long long nout) {
+    const long long qi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= nout) return;
+    long long lo = 0, hi = ntask - 1;
+    while (lo < hi) {
+        const long long mid = (lo + hi + 1) >> 1;
+        if (offset[mid] <= qi) lo = mid;
+        else hi = mid - 1;
+    }
+    const long long k = qi - offset[lo];
+    out[qi] = make_int2(bra[lo], ket_list[ket_start[lo] + k]);
+}
+
+__global__ void fock_build_kernel(int nbf, const double *H, const double *Jacc, const double *Kacc, double *F,
+                                  double *J, double *K) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long n = nbf;
+    if (idx >= n * n) return;
+    const long long r = idx / n, c = idx % n;
+    const double j = 0.5 * (Jacc[r * n + c] + Jacc[c * n + r]);
+    const double k = 0.5 * (Kacc[r * n + c] + Kacc[c * n + r]);
+    if (F) F[idx] = H[idx] + j - 0.5 * k;
+    if (J) J[idx] = j;
+    if (K) K[idx] = k;
+}
+
+__global__ void to_float_kernel(long long n, const double *x, float *y) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = (float)x[i];
+}
+
+}  // namespace sq
+
+using namespace sq;
+
+extern "C" int sq_boys_table(double *table64, float *table32, void *stream) {
+    if (!table64) return set_error(SQ_ERR_ARG, "sq_boys_table: table64 is NULL");
+    const int n = SQ_BOYS_NGRID * SQ_BOYS_NCOL;
+    boys_table_kernel<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(table64, table32);
+    return check_launch("sq_boys_table");
+}
+
+extern "C" int sq_boys(int n_max, const double *z, long long nz, const double *table64, double *out, void *stream) {
+    if (!z || !table64 || !out || nz < 0) return set_error(SQ_ERR_ARG, "sq_boys: bad argument");
+    if (n_max < 0 || n_max > SQ_BOYS_NCOL - 1 - kBoysTaylor64) return set_error(SQ_ERR_ARG, "sq_boys: n_max out of range");
+    if (nz == 0) return SQ_OK;
+    boys_eval_kernel<<<(unsigned)((nz + 127) / 128), 128, 0, (cudaStream_t)stream>>>(n_max, z, nz, table64, out);
+    return check_launch("sq_boys");
+}
+
+extern "C" int sq_pair_prep(const sq_basis *basis, sq_pairs *pairs, void *stream) {
+    if (!basis || !pairs || !pairs->prim || !pairs->herm || !pairs->shells || !pairs->pp_off || !pairs->herm_off)
+        return set_error(SQ_ERR_ARG, "sq_pair_prep: bad argument");
+    if (pairs->nprimpair <= 0) return SQ_OK;
+    pair_prep_kernel<<<(pairs->nprimpair + 127) / 128, 128, 0, (cudaStream_t)stream>>>(*basis, *pairs);
+    return check_launch("sq_pair_prep");
+}
+
+extern "C" int sq_one_electron(const sq_basis *basis, const double *table64, double *S, double *T, double *V,
+                               void *stream) {
+    if (!basis || !table64) return set_error(SQ_ERR_ARG, "sq_one_electron: bad argument");
+    const int np = basis->nshell * (basis->nshell + 1) / 2;
+    if (np == 0) return SQ_OK;
+    one_electron_kernel<<<(np + 63) / 64, 64, 0, (cudaStream_t)stream>>>(*basis, table64, S, T, V);
+    return check_launch("sq_one_electron");
+}
+
+extern "C" int sq_quartets_expand(long long ntask, const int *bra, const int *ket_start, const int *count,
+                                  const long long *offset, const int *ket_list, int *out_pairs, long long nout,
+                                  void *stream) {
+    if (ntask < 0 || nout < 0) return set_error(SQ_ERR_ARG, "sq_quartets_expand: negative size");
+    if (ntask == 0 || nout == 0) return SQ_OK;
+    if (!bra || !ket_start || !count || !offset || !ket_list || !out_pairs)
+        return set_error(SQ_ERR_ARG, "sq_quartets_expand: NULL pointer");
+    quartets_expand_kernel<<<(unsigned)((nout + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+        ntask, bra, ket_start, count, offset, ket_list, (int2 *)out_pairs, nout);
+    return check_launch("sq_quartets_expand");
+}
+
+extern "C" int sq_fock_build(int nbf, const double *H, const double *Jacc, const double *Kacc, double *F, double *J,
+                             double *K, void *stream) {
+    if (nbf <= 0 || !Jacc || !Kacc || (F && !H)) return set_error(SQ_ERR_ARG, "sq_fock_build: bad argument");
+    const long long n2 = (long long)nbf * nbf;
+    fock_build_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, (cudaStream_t)stream>>>(nbf, H, Jacc, Kacc, F, J, K);
+    return check_launch("sq_fock_build");
+}
+
+namespace sq {
+int to_float(long long n, const double *x, float *y, cudaStream_t stream) {
+    if (n <= 0) return SQ_OK;
+    to_float_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, x, y);
+    return check_launch("to_float");
+}
+}  // namespace sq
+
+// ---------------------------------------------------------------------------
+// Arithmetic-pipe probe: independent FMA chains, 16 per thread per iteration.
+namespace sq {
+template <typename T>
+__global__ void fma_probe_kernel(T *out, int iters, T a, T b) {
+    T x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = (T)(threadIdx.x + k);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+    }
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace sq
+
+extern "C" int sq_fma_probe(int precision, int blocks, int iters, void *out, void *stream) {
+    if (blocks <= 0 || iters <= 0 || !out) return set_error(SQ_ERR_ARG, "sq_fma_probe: bad argument");
+    if (precision == SQ_FP64)
+        sq::fma_probe_kernel<double><<<blocks, 256, 0, (cudaStream_t)stream>>>((double *)out, iters, 1.0000001, 1e-9);
+    else
+        sq::fma_probe_kernel<float><<<blocks, 256, 0, (cudaStream_t)stream>>>((float *)out, iters, 1.0000001f, 1e-9f);
+    return check_launch("sq_fma_probe");
+}

@@ -1,0 +1,207 @@
+"""Restricted Hartree-Fock on the GPU: SCF loop, DIIS and the HF class.
+
+Drop-in for slowquant/hartreefock/{hartreefock_in_memory.py, diis.py,
+hartreefockclass.py}: same names, arguments, iteration semantics and log lines.
+Linear algebra runs on the device in FP64 (torch: cuSOLVER eigh, cuBLAS
+products).  The two-electron part comes either from a dense ERI tensor
+(the reference's einsums, hartreefock_in_memory.py:55-56) or from the
+integral-direct J/K kernels (``DirectJK``), optionally in mixed precision.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .logger import _Logger
+
+
+def _dev_tensor(x, device) -> torch.Tensor:
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=torch.float64)
+    return torch.as_tensor(np.asarray(x, dtype=np.float64), device=device)
+
+
+class DIIS:
+    """Pulay DIIS with error FDS - SDF (slowquant/hartreefock/diis.py:4-66)."""
+
+    def __init__(self, number_bf: int, number_fock_saved_: int = 6) -> None:
+        self.fock_matrices: list[torch.Tensor] = []
+        self.density_matrices: list[torch.Tensor] = []
+        self.error_matrices: list[torch.Tensor] = []
+        self.number_fock_saved = number_fock_saved_
+        self.num_bf = number_bf
+        self.last_error: float | None = None
+
+    def get_extrapolated_fock_matrix(self, fock_matrix, density_matrix, S):
+        if len(fock_matrix) == 2:
+            return fock_matrix
+        err = fock_matrix @ density_matrix @ S - S @ density_matrix @ fock_matrix
+        self.last_error = float(err.abs().max())
+        self.fock_matrices.append(fock_matrix)
+        self.density_matrices.append(density_matrix)
+        self.error_matrices.append(err)
+        if len(self.fock_matrices) == 1:
+            return fock_matrix
+        if len(self.fock_matrices) > self.number_fock_saved:
+            self.fock_matrices.pop(0)
+            self.density_matrices.pop(0)
+            self.error_matrices.pop(0)
+        m = len(self.fock_matrices)
+        E = torch.stack(self.error_matrices)  # [m, n, n]
+        # B_ij = trace(e_i e_j) = sum_pq e_i[p,q] e_j[q,p]
+        Bm = torch.einsum("ipq,jqp->ij", E, E)
+        B = torch.zeros((m + 1, m + 1), dtype=torch.float64, device=E.device)
+        B[-1, :] = -1
+        B[:, -1] = -1
+        B[-1, -1] = 0
+        B[:m, :m] = Bm
+        b0 = torch.zeros(m + 1, dtype=torch.float64, device=E.device)
+        b0[-1] = -1
+        coefficients = torch.linalg.solve(B, b0)
+        return torch.einsum("i,ipq->pq", coefficients[:-1], torch.stack(self.fock_matrices))
+
+
+class DirectJK:
+    """Integral-direct J/K callable for run_hartree_fock.
+
+    precision: "fp64", "mixed" (quartets with Schwarz bound < fp32_threshold in
+    FP32 with FP64 Boys recursion) or "mixed_boys32".  In mixed modes the SCF
+    switches to FP64 once the DIIS error max|FDS - SDF| drops below
+    ``fp64_tail_diis_error`` (call ``switch_to_fp64``).
+    """
+
+    def __init__(self, engine, threshold: float = 1e-12, precision: str = "fp64", fp32_threshold: float = 1e-4,
+                 fp64_tail_diis_error: float = 1e-5):
+        self.engine = engine
+        self.threshold = threshold
+        self.precision = precision
+        self.fp32_threshold = fp32_threshold
+        self.fp64_tail_diis_error = fp64_tail_diis_error
+        self.builds: list[str] = []
+
+    @property
+    def mixed(self) -> bool:
+        return self.precision != "fp64"
+
+    def switch_to_fp64(self) -> None:
+        self.precision = "fp64"
+
+    def __call__(self, D: torch.Tensor):
+        self.builds.append(self.precision)
+        return self.engine.jk(D, self.threshold, self.precision, self.fp32_threshold)
+
+
+def run_hartree_fock(S, T, V, ERI, number_electrons: int, log, dE_threshold: float, rmsd_threshold: float,
+                     max_scf_iterations: int, use_diis: bool = True):
+    """Restricted Hartree-Fock (hartreefock_in_memory.py:7-94).
+
+    ERI is a dense (nbf,)*4 tensor (numpy or torch) or a callable D -> (J, K)
+    such as DirectJK.  Returns (E_elec, C, F, D) as numpy arrays.
+    """
+    device = torch.device("cuda", torch.cuda.current_device())
+    log.add_to_log(f"{'Iter':^4}    {'E_HF':^18}    {'DeltaE':^13}    {'RMS_D':^12}")
+    S = _dev_tensor(S, device)
+    Hcore = _dev_tensor(T, device) + _dev_tensor(V, device)
+    if callable(ERI):
+        jk = ERI
+    else:
+        G = _dev_tensor(ERI, device)
+
+        def jk(D):
+            return torch.einsum("pqrs,sr->pq", G, D), torch.einsum("psqr,sr->pq", G, D)
+
+    Lambda_S, L_S = torch.linalg.eigh(S)
+    S_sqrt = L_S @ torch.diag(Lambda_S ** (-1 / 2)) @ L_S.T
+    F0prime = S_sqrt.T @ Hcore @ S_sqrt.T
+    _, C0prime = torch.linalg.eigh(F0prime)
+    C0 = (S_sqrt @ C0prime).T
+    nocc = int(number_electrons / 2)
+    C0 = C0[0:nocc]
+    D0 = 2 * C0.T @ C0
+    E0 = torch.sum(D0 * Hcore)
+    number_bf = len(S)
+    diis_acceleration = DIIS(number_bf) if use_diis else None
+    mixed = getattr(jk, "mixed", False)
+    for iteration in range(1, max_scf_iterations + 1):
+        J, K = jk(D0)
+        F = Hcore + J - 0.5 * K
+        if diis_acceleration is not None:
+            F = diis_acceleration.get_extrapolated_fock_matrix(F, D0, S)
+            if mixed and getattr(jk, "mixed", False):
+                err = diis_acceleration.last_error
+                if err is not None and err < jk.fp64_tail_diis_error:
+                    jk.switch_to_fp64()
+                    diis_acceleration = DIIS(number_bf)
+        elif mixed and getattr(jk, "mixed", False):
+            err = float((F @ D0 @ S - S @ D0 @ F).abs().max())
+            if err < jk.fp64_tail_diis_error:
+                jk.switch_to_fp64()
+        Fprime = S_sqrt.T @ F @ S_sqrt
+        _, Cprime = torch.linalg.eigh(Fprime)
+        C = S_sqrt @ Cprime
+        Cocc = C[:, 0:nocc]
+        D = 2 * Cocc @ Cocc.T
+        E = 0.5 * torch.sum(D * (Hcore + F))
+        dE = float(E - E0)
+        rmsd = float(torch.sum((D - D0) ** 2) ** 0.5)
+        Ef = float(E)
+        log.add_to_log(f"{iteration:>4}    {Ef: 18.12f}    {dE: 1.6e}    {rmsd:1.6e}")
+        D0 = D
+        E0 = E
+        still_mixed = mixed and getattr(jk, "mixed", False)
+        if np.abs(dE) < dE_threshold and rmsd < rmsd_threshold and not still_mixed:
+            break
+    else:
+        log.add_to_log(
+            f"Restricted Hartree-Fock did not meet convergence requirements in {max_scf_iterations} iterations",
+            is_warning=True,
+        )
+    return float(E), C.cpu().numpy(), F.cpu().numpy(), D.cpu().numpy()
+
+
+class _HartreeFock:
+    """HF driver (hartreefockclass.py:14-152, restricted part).
+
+    Extra knobs beyond the reference: ``direct_jk`` (default True: integral-
+    direct Fock builds instead of the stored ERI tensor), ``precision``
+    ("fp64" | "mixed" | "mixed_boys32"), ``fp32_schwarz_threshold``,
+    ``fp64_tail_diis_error``.
+    """
+
+    def __init__(self, molecule_obj, integral_obj) -> None:
+        self.mol_obj = molecule_obj
+        self.int_obj = integral_obj
+        self.de_threshold = 10**-9
+        self.rmsd_threshold = 10**-9
+        self.max_scf_iterations = 100
+        self.uhf_lumo_homo_mix_coeff = 0.15
+        self.use_diis = True
+        self.logger = _Logger()
+        self.direct_jk = True
+        self.precision = "fp64"
+        self.fp32_schwarz_threshold = 1e-4
+        self.fp64_tail_diis_error = 1e-5
+        self.fock_builds: list[str] = []
+
+    @property
+    def log(self) -> str:
+        return self.logger.log
+
+    def run_restricted_hartree_fock(self) -> None:
+        if self.direct_jk:
+            eri = DirectJK(self.int_obj.engine, self.int_obj.cauchy_schwarz_threshold, self.precision,
+                           self.fp32_schwarz_threshold, self.fp64_tail_diis_error)
+            S, T, V = self.int_obj.one_electron_device()
+        else:
+            eri = self.int_obj.electron_repulsion_tensor
+            S, T, V = (self.int_obj.overlap_matrix, self.int_obj.kinetic_energy_matrix,
+                       self.int_obj.nuclear_attraction_matrix)
+        E, C, F, D = run_hartree_fock(S, T, V, eri, self.mol_obj.number_electrons, self.logger, self.de_threshold,
+                                      self.rmsd_threshold, self.max_scf_iterations, self.use_diis)
+        if self.direct_jk:
+            self.fock_builds = list(eri.builds)
+        self.E_hf = E
+        self.mo_coeff = C
+        self.rdm1 = D
+        self.fock_matrix = F

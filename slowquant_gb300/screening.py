@@ -1,0 +1,134 @@
+"""Schwarz screening and shell-quartet work-list construction (host side).
+
+Replaces the shell-quartet loops of electron_repulsion_integral_driver
+(slowquant/molecularintegrals/electronrepulsion.py:32-49): the reference visits
+i <= j, k <= l with "ij >= kl" and skips a quartet when
+cs[i,j] * cs[k,l] < threshold.  Here the unique quartets are enumerated as
+(bra pair, ket pair) combinations of pair *groups*:
+
+* a group is the set of shell pairs with the same pair class (la, lb) and the
+  same primitive counts, sorted by descending Schwarz factor q;
+* bra group g1 meets ket groups g2 <= g1 whose class is not above g1's class
+  (so bra class >= ket class), and inside one group only ket position <= bra
+  position, which makes every unordered pair of pairs appear once;
+* for a bra pair with factor x the surviving kets of a group are the prefix
+  with x * q_ket >= threshold (the same product test as the reference), and
+  with a second threshold that prefix splits into a large-bound (FP64) part
+  and a small-bound (FP32) part.
+
+``build_tasks`` returns per quartet class the (bra pair, ket start, count)
+tasks; the device kernel sq_quartets_expand turns them into the flat list.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+NQCLASS = 21
+
+
+def quartet_class(cb: int, ck: int) -> int:
+    return cb * (cb + 1) // 2 + ck
+
+
+def prefix_counts(x: np.ndarray, qk: np.ndarray, thr: float) -> np.ndarray:
+    """For each bra factor x: number of leading ket factors (descending qk) with x*qk >= thr."""
+    n = len(qk)
+    if n == 0 or len(x) == 0:
+        return np.zeros(len(x), dtype=np.int64)
+    with np.errstate(divide="ignore", over="ignore"):
+        lim = np.where(x > 0, thr / np.where(x > 0, x, 1.0), np.inf)
+    cnt = np.searchsorted(-qk, -lim, side="right").astype(np.int64)
+    # exact product test at the boundary, the comparison the reference uses
+    for _ in range(4):
+        dec = (cnt > 0) & (x * qk[np.clip(cnt - 1, 0, n - 1)] < thr)
+        cnt = np.where(dec, cnt - 1, cnt)
+        inc = (cnt < n) & (x * qk[np.clip(cnt, 0, n - 1)] >= thr)
+        cnt = np.where(inc, cnt + 1, cnt)
+    return cnt
+
+
+def pair_groups(pair_class: np.ndarray, npa: np.ndarray, npb: np.ndarray, q: np.ndarray):
+    """[(class, member pair indices sorted by descending q)], ordered by (class, npa, npb)."""
+    keys = np.stack([pair_class, npa, npb], axis=1)
+    if len(keys) == 0:
+        return []
+    uniq = np.unique(keys, axis=0)
+    groups = []
+    for k in uniq:
+        idx = np.nonzero((keys == k).all(axis=1))[0]
+        idx = idx[np.argsort(-q[idx], kind="stable")]
+        groups.append((int(k[0]), idx.astype(np.int32)))
+    return groups
+
+
+def build_tasks(pair_class, npa, npb, q, threshold: float, fp32_threshold: float | None = None):
+    """Tasks per list and quartet class.
+
+    Returns (lists, ket_list): lists[li][qc] = list of (bra ids, ket starts,
+    counts) arrays, li = 0 for the FP64 (or only) list, 1 for the FP32 list;
+    ket_list is the concatenation of the groups' sorted members.
+    """
+    q = np.asarray(q, dtype=np.float64)
+    groups = pair_groups(np.asarray(pair_class), np.asarray(npa), np.asarray(npb), q)
+    ket_list = np.concatenate([g[1] for g in groups]).astype(np.int32) if groups else np.zeros(0, np.int32)
+    gstart = np.concatenate([[0], np.cumsum([len(g[1]) for g in groups])]).astype(np.int64)
+    nlists = 1 if fp32_threshold is None else 2
+    lists = [{c: [] for c in range(NQCLASS)} for _ in range(nlists)]
+    for g1, (c1, m1) in enumerate(groups):
+        x = q[m1]
+        for g2 in range(g1 + 1):
+            c2, m2 = groups[g2]
+            if c2 > c1:
+                continue
+            qk = q[m2]
+            cnt = prefix_counts(x, qk, threshold)
+            if g2 == g1:
+                cnt = np.minimum(cnt, np.arange(1, len(m1) + 1))
+            if fp32_threshold is None:
+                bounds = [(np.zeros_like(cnt), cnt)]
+            else:
+                c64 = np.minimum(prefix_counts(x, qk, fp32_threshold), cnt)
+                bounds = [(np.zeros_like(cnt), c64), (c64, cnt)]
+            qc = quartet_class(c1, c2)
+            for li, (lo, hi) in enumerate(bounds):
+                n = hi - lo
+                keep = n > 0
+                if keep.any():
+                    lists[li][qc].append((m1[keep], gstart[g2] + lo[keep], n[keep]))
+    return lists, ket_list
+
+
+def flatten_tasks(tasks: dict):
+    """Concatenate one list's tasks: (bra, ket_start, count, task offsets, class offsets)."""
+    bra, kst, cnt = [], [], []
+    off = np.zeros(NQCLASS + 1, dtype=np.int64)
+    for c in range(NQCLASS):
+        tot = 0
+        for m, s, n in tasks[c]:
+            bra.append(m)
+            kst.append(s)
+            cnt.append(n)
+            tot += int(n.sum())
+        off[c + 1] = off[c] + tot
+    if bra:
+        bra = np.concatenate(bra).astype(np.int32)
+        kst = np.concatenate(kst).astype(np.int32)
+        cnt = np.concatenate(cnt).astype(np.int64)
+    else:
+        bra = np.zeros(0, np.int32)
+        kst = np.zeros(0, np.int32)
+        cnt = np.zeros(0, np.int64)
+    toff = np.concatenate([[0], np.cumsum(cnt)[:-1]]).astype(np.int64) if len(cnt) else np.zeros(0, np.int64)
+    return bra, kst, cnt, toff, off
+
+
+def expand_host(bra, kst, cnt, ket_list) -> np.ndarray:
+    """Host restatement of sq_quartets_expand (for tests and small checks)."""
+    if len(bra) == 0:
+        return np.zeros((0, 2), dtype=np.int32)
+    rep_bra = np.repeat(bra, cnt)
+    starts = np.repeat(kst.astype(np.int64), cnt)
+    first = np.repeat(np.concatenate([[0], np.cumsum(cnt)[:-1]]), cnt)
+    k = np.arange(int(cnt.sum())) - first
+    return np.stack([rep_bra, ket_list[starts + k]], axis=1).astype(np.int32)

@@ -1,0 +1,141 @@
+"""GPU integral kernels against the oracle and the reference's golden outputs.
+
+Tolerances: integrals 1e-10 absolute (the parity bar), Boys 1e-12.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.conftest import load_golden, unpack_unique
+
+pytestmark = pytest.mark.gpu
+
+SYSTEMS = ["h2o_sto3g_crawford", "h2o_sto3g_c1", "ch4_sto3g", "h2o_631gs", "h2o_dz", "h2o_ccpvdz_c1", "h2o_dzp",
+           "h6_dzp"]
+
+
+def _engine(geom, basis, unit):
+    from slowquant_gb300.engine import IntegralEngine
+    from slowquant_gb300.molecule import _Molecule
+
+    m = _Molecule(geom, 0, unit)
+    m._set_basis_set(basis)
+    return IntegralEngine(m)
+
+
+@pytest.fixture(autouse=True)
+def _lib_ready(gpu_lib):
+    from slowquant_gb300 import _lib
+
+    _lib.lib().sq_set_option(_lib.SQ_OPT_GENERIC_MIN_L, 5)
+    yield
+    _lib.lib().sq_set_option(_lib.SQ_OPT_GENERIC_MIN_L, 5)
+
+
+def test_boys_against_oracle():
+    import torch
+
+    from slowquant_gb300 import _lib
+
+    eng = _engine("H 0 0 0;H 0 0 1.4", "sto-3g", "bohr")
+    z = np.concatenate([[0.0, 1e-14, 1e-9, 1e-4], np.linspace(0.001, 60, 1777), [35.99, 36.0, 36.01, 100.0, 1e4]])
+    nmax = 8
+    zt = torch.tensor(z, dtype=torch.float64, device="cuda")
+    out = torch.zeros((len(z), nmax + 1), dtype=torch.float64, device="cuda")
+    _lib.check(_lib.lib().sq_boys(nmax, zt.data_ptr(), len(z), eng.tab64.data_ptr(), out.data_ptr(),
+                                  _lib.stream_handle()), "sq_boys")
+    got = out.cpu().numpy()
+    ref = np.array([[O.boys(n, zz) for n in range(nmax + 1)] for zz in z])
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12)
+    # away from the reference's z > 25 asymptotic switch both are exact to ~1e-14 relative
+    sel = (z < 24.0) | (z > 45.0)
+    np.testing.assert_allclose(got[sel], ref[sel], rtol=2e-13, atol=1e-300)
+
+
+@pytest.mark.parametrize("name", SYSTEMS)
+def test_schwarz_dense_eri_one_electron(name, golden_energies):
+    e = golden_energies[name]
+    d = load_golden(name)
+    eng = _engine(e["geometry"], e["basis"], e["unit"])
+    np.testing.assert_allclose(eng.schwarz_matrix(), d["schwarz"], atol=1e-12)
+    V = eng.eri_dense(1e-12).cpu().numpy()
+    ref = d["eri"] if "eri" in d else unpack_unique(d["eri_unique"], eng.nbf)
+    np.testing.assert_allclose(V, ref, atol=1e-10)
+    assert np.max(np.abs(V - ref)) < 1e-11
+    S, T, Vn = (x.cpu().numpy() for x in eng.one_electron())
+    np.testing.assert_allclose(S, d["S"], atol=1e-12)
+    np.testing.assert_allclose(T, d["T"], atol=1e-11)
+    np.testing.assert_allclose(Vn, d["V"], atol=1e-10)
+
+
+def _random_density(n, seed):
+    rng = np.random.default_rng(seed)
+    C = rng.normal(size=(n, max(1, n // 3))) / np.sqrt(n)
+    return 2 * C @ C.T
+
+
+@pytest.mark.parametrize("geom_kind", ["monomer_ccpvdz", "dimer_ccpvdz", "trimer_631gs"])
+def test_direct_jk_matches_oracle_einsum(geom_kind):
+    import torch
+
+    from slowquant_gb300 import systems
+
+    geom, basis = {
+        "monomer_ccpvdz": (systems.water_monomer(), "cc-pvdz"),
+        "dimer_ccpvdz": (systems.water_cluster(2, 5.0, seed=2), "cc-pvdz"),
+        "trimer_631gs": (systems.water_cluster(3, 6.0, seed=3), "6-31G*"),
+    }[geom_kind]
+    o = O.OracleMolecule(geom, basis, "angstrom")
+    Vref = o.eri_dense(1e-12)
+    eng = _engine(geom, basis, "angstrom")
+    D = _random_density(eng.nbf, 5)
+    Jr, Kr = O.jk_from_eri(Vref, D)
+    Dt = torch.tensor(D, dtype=torch.float64, device="cuda")
+    J, K = (x.cpu().numpy() for x in eng.jk(Dt, 1e-12, "fp64"))
+    np.testing.assert_allclose(J, Jr, atol=1e-10)
+    np.testing.assert_allclose(K, Kr, atol=1e-10)
+
+
+def test_generic_warp_kernel_matches_per_class_kernels():
+    """Every class on the warp kernel == the unrolled per-class kernels (J/K)."""
+    import torch
+
+    from slowquant_gb300 import _lib, systems
+
+    eng = _engine(systems.water_cluster(2, 5.0, seed=2), "cc-pvdz", "angstrom")
+    D = torch.tensor(_random_density(eng.nbf, 1), dtype=torch.float64, device="cuda")
+    J1, K1 = (x.cpu().numpy() for x in eng.jk(D, 1e-12, "fp64"))
+    _lib.lib().sq_set_option(_lib.SQ_OPT_GENERIC_MIN_L, 0)
+    J2, K2 = (x.cpu().numpy() for x in eng.jk(D, 1e-12, "fp64"))
+    np.testing.assert_allclose(J2, J1, atol=1e-11)
+    np.testing.assert_allclose(K2, K1, atol=1e-11)
+    # FP32 paths of both kernels agree with FP64 within the FP32 error scale
+    for prec in ("mixed", "mixed_boys32"):
+        for min_l in (0, 5):
+            _lib.lib().sq_set_option(_lib.SQ_OPT_GENERIC_MIN_L, min_l)
+            J3, K3 = (x.cpu().numpy() for x in eng.jk(D, 1e-12, prec, fp32_threshold=1e30))
+            assert np.max(np.abs(J3 - J1)) < 1e-4
+            assert np.max(np.abs(K3 - K1)) < 1e-4
+
+
+def test_driver_entry_points_follow_reference_screening():
+    """electronrepulsion.py semantics: no matrix -> all quartets; huge threshold -> zeros."""
+    from slowquant_gb300 import electronrepulsion as er
+    from slowquant_gb300.molecule import _Molecule
+
+    g = "H 0 0 0;H 1 0 0;H 2 0 0;H 3 0 0;H 4 0 0;H 5 0 0"
+    m = _Molecule(g, 0, "bohr")
+    m._set_basis_set("dzp")
+    cs = er.get_cauchy_schwarz_matrix(m)
+    d = load_golden("h6_dzp")
+    np.testing.assert_allclose(cs, d["schwarz"], atol=1e-12)
+    full = er.electron_repulsion_integral_driver(m)
+    ref = unpack_unique(d["eri_unique"], m.number_bf)
+    np.testing.assert_allclose(full, ref, atol=1e-10)
+    for thr, tol in [(1e-8, 1e-8), (1e-3, 1e-3)]:
+        Vs = er.electron_repulsion_integral_driver(m, cs, thr)
+        np.testing.assert_allclose(Vs, full, atol=tol)
+    assert np.all(er.electron_repulsion_integral_driver(m, cs, 1e10) == 0.0)

@@ -1,0 +1,139 @@
+"""Host-side logic on CPU: molecule/basis layer, screening work lists, C ABI exports."""
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from slowquant_gb300 import molecule, screening, systems
+from tests.conftest import ROOT, load_golden
+
+
+def test_molecule_matches_oracle_restatement():
+    geom = systems.water_cluster(3, 6.0, seed=3)
+    m = molecule._Molecule(geom, 0, "angstrom")
+    m._set_basis_set("cc-pvdz")
+    o = O.OracleMolecule(geom, "cc-pvdz", "angstrom")
+    assert m.number_bf == o.nbf == 75
+    assert m.number_shell == len(o.shells) == 36
+    assert m.number_electrons == o.number_electrons == 30
+    assert abs(m.nuclear_repulsion - o.nuclear_repulsion) < 1e-10
+    for s, t in zip(m.shells, o.shells):
+        np.testing.assert_allclose(s.normalization, t[4], rtol=1e-13)
+        np.testing.assert_array_equal(s.angular_moments, t[3])
+
+
+def test_normalization_factorises_per_component():
+    """N[bf,i] = g(alpha_i) / sqrt((2x-1)!!(2y-1)!!(2z-1)!!): the identity the kernels use."""
+    m = molecule._Molecule(systems.water_monomer(), 0, "angstrom")
+    m._set_basis_set("cc-pvdz")
+    g = load_golden("primitives")
+    np.testing.assert_allclose(np.concatenate([s.normalization.ravel() for s in m.shells]), g["ccpvdz_h2o_norms"],
+                               rtol=1e-13)
+    for s in m.shells:
+        base = s.component_independent_coefficients()
+        for b, ang in enumerate(s.angular_moments):
+            df = np.prod([molecule.factorial2(2 * a - 1) for a in ang])
+            np.testing.assert_allclose(base / np.sqrt(df), s.contraction_coefficients * s.normalization[b], rtol=1e-13)
+
+
+def test_molecule_errors_follow_reference():
+    with pytest.raises(ValueError):
+        molecule._Molecule("H 0 0 0;H 0 0 1", 0, "parsec")
+    with pytest.raises(ValueError):
+        molecule._Molecule("H 0 0 0", 0, "bohr")
+    m = molecule._Molecule("Xe 0 0 0;", 0, "bohr")
+    with pytest.raises(ValueError):
+        m._set_basis_set("cc-pvdz")
+    m = molecule._Molecule("H 0 0 0;H 0 0 1.4;", 0, "bohr")
+    m._set_basis_set("6-31G**")
+    assert m.number_bf == 10
+
+
+def test_angstrom_factor_and_geometries():
+    m = molecule._Molecule("H 0 0 0;H 0 0 1", 0, "angstrom")
+    assert m.atom_coordinates[1, 2] == 1.889725989
+    c = systems.water_cluster(16, 11.0, seed=16)
+    xyz = np.array([[float(v) for v in a.split()[1:]] for a in c.split(";")])
+    o = xyz[0::3]
+    d = np.linalg.norm(o[:, None] - o[None], axis=-1) + np.eye(len(o)) * 10
+    assert d.min() >= 2.7 and xyz.min() > -1.0 and xyz.max() < 12.0
+    oh = np.linalg.norm(xyz[1::3] - o, axis=1)
+    np.testing.assert_allclose(oh, 0.96, atol=1e-9)
+    assert len(systems.octane().split(";")) == 26
+    assert len(systems.hydrogen_chain(24, seed=24).split(";")) == 24
+
+
+def _brute_force(pc, q, thr):
+    n = len(q)
+    out = set()
+    for P in range(n):
+        for Q in range(n):
+            if pc[Q] > pc[P] or (pc[Q] == pc[P] and Q > P):
+                continue
+            if q[P] * q[Q] >= thr:
+                out.add((P, Q))
+    return out
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_quartet_lists_unique_and_complete(seed):
+    rng = np.random.default_rng(seed)
+    n = 60
+    pc = np.sort(rng.integers(0, 6, n)).astype(np.int32)
+    npa = rng.choice([1, 3, 8], n)
+    npb = rng.choice([1, 3], n)
+    q = 10.0 ** rng.uniform(-9, 0.5, n)
+    thr = 1e-6
+    lists, ket = screening.build_tasks(pc, npa, npb, q, thr)
+    bra, kst, cnt, toff, off = screening.flatten_tasks(lists[0])
+    pairs = screening.expand_host(bra, kst, cnt, ket)
+    got = {tuple(sorted(p, key=lambda x: (pc[x], x), reverse=True)) for p in pairs}
+    assert len(got) == len(pairs)  # no quartet twice
+    ref = {tuple(sorted(p, key=lambda x: (pc[x], x), reverse=True)) for p in _brute_force(pc, q, thr)}
+    assert got == ref
+    # each class segment holds only its class, bra class >= ket class
+    for c in range(screening.NQCLASS):
+        seg = pairs[off[c]:off[c + 1]]
+        for P, Q in seg:
+            assert screening.quartet_class(pc[P], pc[Q]) == c and pc[P] >= pc[Q]
+    # the fp64 / fp32 split partitions the same set by the bound
+    l2, ket2 = screening.build_tasks(pc, npa, npb, q, thr, fp32_threshold=1e-3)
+    p64 = screening.expand_host(*screening.flatten_tasks(l2[0])[:3], ket2)
+    p32 = screening.expand_host(*screening.flatten_tasks(l2[1])[:3], ket2)
+    assert len(p64) + len(p32) == len(pairs)
+    assert np.all(q[p64[:, 0]] * q[p64[:, 1]] >= 1e-3)
+    assert np.all(q[p32[:, 0]] * q[p32[:, 1]] < 1e-3)
+
+
+def test_screening_boundary_uses_product_test():
+    q = np.array([1e-3, 1e-3 * (1 + 1e-16), 2e-3])
+    x = np.array([1e-3])
+    thr = float(x[0] * q[0])
+    c = screening.prefix_counts(x, np.sort(q)[::-1], thr)
+    assert c[0] == int(np.sum(x[0] * q >= thr))
+
+
+def _header_functions():
+    text = open(os.path.join(ROOT, "include", "slowquant_gb300.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:[A-Za-z_]\w*[\s*]+)+(sq_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_header_declares_bound_entry_points():
+    from slowquant_gb300 import _lib
+
+    assert set(_header_functions()) == set(_lib.EXPORTED)
+
+
+def test_library_exports_every_header_symbol():
+    from slowquant_gb300 import _lib, build
+
+    if not os.path.exists(_lib.LIB_PATH):
+        build.build()
+    lib = ctypes.CDLL(_lib.LIB_PATH)
+    for name in _header_functions():
+        assert hasattr(lib, name), name
+    assert lib.sq_version() >= 1

@@ -1,0 +1,99 @@
+"""The oracle (C restatement of the reference) against the reference's own outputs.
+
+The golden fixtures were produced by running the reference package
+(tests/golden/make_golden.py); the known-answer energies are the reference
+test suite's literature values (tests/test_hartreefock.py of the reference).
+"""
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.conftest import load_golden, unpack_unique
+
+SYSTEMS = ["h2o_sto3g_crawford", "h2o_sto3g_c1", "ch4_sto3g", "h2o_631gs", "h2o_dz", "h2o_ccpvdz_c1", "h2o_dzp"]
+
+
+def test_boys_grid_matches_reference():
+    g = load_golden("primitives")
+    F = np.array([[O.boys(int(n), float(z)) for z in g["boys_z"]] for n in g["boys_n"]])
+    np.testing.assert_allclose(F, g["boys_F"], rtol=1e-14, atol=0)
+
+
+def test_expansion_and_hermite_match_reference():
+    import ctypes
+
+    g = load_golden("primitives")
+    lib = O.lib()
+    vals = []
+    for A_x, B_x, a, b, la, lb in g["ecoef_params"]:
+        la, lb = int(la), int(lb)
+        out = np.zeros((la + 1) * (lb + 1) * (la + lb + 1))
+        lib.sqo_expansion_coefficients(ctypes.c_double(A_x), ctypes.c_double(B_x), ctypes.c_double(a),
+                                       ctypes.c_double(b), la, lb, out.ctypes.data_as(ctypes.c_void_p))
+        vals.append(out)
+    np.testing.assert_allclose(np.concatenate(vals), g["ecoef_values"], rtol=1e-13, atol=1e-15)
+    vals = []
+    for L, p, x, y, z in g["hermite_params"]:
+        L = int(L)
+        out = np.zeros((L + 1) ** 3)
+        PC = np.array([x, y, z])
+        lib.sqo_hermite_coulomb(L, L, L, ctypes.c_double(p), PC.ctypes.data_as(ctypes.c_void_p),
+                                out.ctypes.data_as(ctypes.c_void_p))
+        vals.append(out)
+    # the recurrence cancels strongly for large p; ulp-level Boys differences grow to ~1e-11
+    np.testing.assert_allclose(np.concatenate(vals), g["hermite_values"], rtol=1e-10, atol=1e-14)
+
+
+def test_normalization_matches_reference():
+    from slowquant_gb300.systems import water_monomer
+
+    g = load_golden("primitives")
+    m = O.OracleMolecule(water_monomer(), "cc-pvdz", "angstrom")
+    norms = np.concatenate([s[4].ravel() for s in m.shells])
+    np.testing.assert_allclose(norms, g["ccpvdz_h2o_norms"], rtol=1e-13)
+
+
+@pytest.mark.parametrize("name", SYSTEMS)
+def test_oracle_integrals_and_energy(name, golden_energies):
+    e = golden_energies[name]
+    d = load_golden(name)
+    m = O.OracleMolecule(e["geometry"], e["basis"], e["unit"])
+    assert m.nbf == e["nbf"]
+    assert abs(m.nuclear_repulsion - e["E_nuc"]) < 1e-12
+    cs = m.schwarz()
+    np.testing.assert_allclose(cs, d["schwarz"], atol=1e-12)
+    V = m.eri_dense(1e-12)
+    ref = d["eri"] if "eri" in d else unpack_unique(d["eri_unique"], m.nbf)
+    np.testing.assert_allclose(V, ref, atol=1e-12)
+    S, T, Vn = m.one_electron()
+    np.testing.assert_allclose(S, d["S"], atol=1e-12)
+    np.testing.assert_allclose(T, d["T"], atol=1e-12)
+    np.testing.assert_allclose(Vn, d["V"], atol=1e-11)
+    E, C, F, D, its = O.run_hartree_fock(S, T, Vn, lambda Dm: O.jk_from_eri(V, Dm), m.number_electrons)
+    assert abs(E - e["E_hf"]) < 1e-10
+    assert len(its) == e["n_iter"]
+    # early iterations follow the same trajectory; later ones pass through DIIS
+    # solves that can be nearly singular (e.g. Td CH4), so only the end point is tight
+    np.testing.assert_allclose(its[:4], e["scf_energies"][:4], atol=1e-9)
+
+
+def test_oracle_faithful_mode_identical():
+    """The reference's (L,L,L) Hermite table and the triangular one give the same ERIs."""
+    from slowquant_gb300.systems import water_monomer
+
+    m = O.OracleMolecule(water_monomer(), "6-31G*", "angstrom")
+    Vf = m.eri_dense(1e-12, faithful=True)
+    Vt = m.eri_dense(1e-12, faithful=False)
+    np.testing.assert_allclose(Vf, Vt, atol=1e-13)
+
+
+@pytest.mark.parametrize("name,ref", [
+    ("h2o_sto3g_crawford", -82.944446990003),
+    ("h2o_dz", -83.980246037187),
+    ("h2o_dzp", -84.01054766778844),
+    ("ch4_sto3g", -53.224154786383),
+])
+def test_reference_known_answers(name, ref, golden_energies):
+    """The reference suite's literature energies (1e-6 Eh) hold for its own output."""
+    assert abs(golden_energies[name]["E_hf"] - ref) < 1e-6
