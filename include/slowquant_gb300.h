@@ -103,9 +103,11 @@ long long sq_get_option(int key);
  * (slowquant/molecularintegrals/integralfunctions.py:74-97). */
 int sq_boys_table(double *table64, float *table32, void *stream);
 
-/* F_0..F_{n_max}(z[i]) for nz arguments -> out[nz][n_max+1].  Test hook for
- * boys_function (integralfunctions.py:74-97). */
-int sq_boys(int n_max, const double *z, long long nz, const double *table64, double *out, void *stream);
+/* F_0..F_{n_max}(z[i]) for nz arguments -> out[nz][n_max+1]; n_max <= 8.
+ * mode 0: the tabulated function the J/K kernels use; mode 1: the reference's
+ * piecewise formula that the dense-tensor and Schwarz kernels use.  Test hook
+ * for boys_function (integralfunctions.py:74-97). */
+int sq_boys(int n_max, const double *z, long long nz, const double *table64, int mode, double *out, void *stream);
 
 /* Primitive-pair data for every pair in `pairs`: P, p, U and the Hermite
  * expansion coefficients of expansion_coefficients

@@ -60,10 +60,36 @@ double sqo_factorial2(double number) {
     return out;
 }
 
+/*
+ * Boys-function mode: 0 (default) restates the reference's piecewise formula
+ * exactly; 1 evaluates the same series to full double precision (relative
+ * stopping test, asymptote only beyond z = 40).  Mode 1 exists to measure how
+ * far the reference's own truncation moves the integrals.
+ */
+static int g_boys_mode = 0;
+void sqo_set_boys_mode(int mode) { g_boys_mode = mode; }
+
+static double boys_exact(int n, double z) {
+    const double pi = 3.141592653589793;
+    if (z > 40.0) {
+        double F = 0.5 * sqrt(pi / z);
+        for (int m = 0; m < n; m++) F *= (2 * m + 1) / (2.0 * z);
+        return F;
+    }
+    double term = 1.0 / (2 * n + 1), sum = 0.0;
+    for (int i = 0; i < 2000; i++) {
+        sum += term;
+        term *= 2.0 * z / (2 * n + 2 * i + 3);
+        if (term < 1e-18 * sum) break;
+    }
+    return sum * exp(-z);
+}
+
 /* integralfunctions.py:74-97 */
 double sqo_boys(int n, double z) {
     const double pi = 3.141592653589793;
     double F;
+    if (g_boys_mode == 1) return boys_exact(n, z);
     if (n == 0 && z < 1e-10) {
         F = 1.0;
     } else if (n == 0) {

@@ -71,7 +71,7 @@ def lib() -> ctypes.CDLL:
         L.sq_get_option.argtypes = [ctypes.c_int]
         L.sq_set_option.argtypes = [ctypes.c_int, ctypes.c_longlong]
         L.sq_boys_table.argtypes = [_p, _p, _p]
-        L.sq_boys.argtypes = [ctypes.c_int, _p, ctypes.c_longlong, _p, _p, _p]
+        L.sq_boys.argtypes = [ctypes.c_int, _p, ctypes.c_longlong, _p, ctypes.c_int, _p, _p]
         L.sq_pair_prep.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), _p]
         L.sq_schwarz.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqQuartets), _p,
                                  _p, _p]

@@ -29,7 +29,7 @@
 namespace sq {
 
 enum { MODE_DENSE = 0, MODE_SCHWARZ = 1, MODE_JK = 2 };
-enum { BOYS_FP64 = 0, BOYS_FP32 = 1 };
+enum { BOYS_FP64 = 0, BOYS_FP32 = 1, BOYS_REF = 2 };
 
 struct EriArgs {
     sq_basis basis;

@@ -9,6 +9,8 @@
 //     warp-private shared-memory buffer;
 //   * the ket transform W[h][cd] += sum (-1)^{tau+nu+phi} E^{cd}_{tau nu phi}
 //     R[h + (tau,nu,phi)] is spread over lanes by output entry (cd-major).
+// Dense-tensor and Schwarz launches evaluate each F_m with the reference's own
+// piecewise formula (boys_reference), J/K launches with the tabulated one.
 // After the ket primitive loop the bra transform (ab|cd) += sum_h E^{ab}_h W[h][cd]
 // runs with lanes owning output entries, accumulated in registers.  The
 // arithmetic is that of the per-thread kernel (eri.cuh); the class is a
@@ -159,7 +161,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
                 if (lane <= L) {
                     R Fm;
                     const int m = lane;
-                    if constexpr (std::is_same<R, double>::value || BOYS == BOYS_FP64) {
+                    if constexpr (BOYS == BOYS_REF) {
+                        Fm = (R)boys_reference(m, (double)T);
+                    } else if constexpr (std::is_same<R, double>::value || BOYS == BOYS_FP64) {
                         const double Td = (double)T;
                         double f;
                         if (Td < SQ_BOYS_TMAX) {
@@ -350,10 +354,11 @@ inline cudaError_t launch_eri_warp(const EriArgs &args, const WarpClass &cls, in
         if (e != cudaSuccess) return e;                                                                         \
         kern<<<grid, block, sz, stream>>>(args, cls);                                                           \
     } while (0)
+    // Dense tensors and Schwarz factors are drop-in outputs: reference-compatible Boys.
     if (mode == MODE_DENSE)
-        SQ_WARP_LAUNCH(double, BOYS_FP64, MODE_DENSE);
+        SQ_WARP_LAUNCH(double, BOYS_REF, MODE_DENSE);
     else if (mode == MODE_SCHWARZ)
-        SQ_WARP_LAUNCH(double, BOYS_FP64, MODE_SCHWARZ);
+        SQ_WARP_LAUNCH(double, BOYS_REF, MODE_SCHWARZ);
     else if (precision == SQ_FP64)
         SQ_WARP_LAUNCH(double, BOYS_FP64, MODE_JK);
     else if (precision == SQ_FP32)

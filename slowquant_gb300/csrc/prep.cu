@@ -35,11 +35,16 @@ __global__ void boys_table_kernel(double *tab64, float *tab32) {
     if (tab32) tab32[idx] = (float)val;
 }
 
-__global__ void boys_eval_kernel(int n_max, const double *z, long long nz, const double *tab, double *out) {
+__global__ void boys_eval_kernel(int n_max, const double *z, long long nz, const double *tab, int mode,
+                                 double *out) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nz) return;
     double F[SQ_BOYS_NCOL];
-    boys64_rt(n_max, z[i], tab, F);
+    if (mode == 1) {
+        for (int m = 0; m <= n_max; ++m) F[m] = boys_reference(m, z[i]);
+    } else {
+        boys64_rt(n_max, z[i], tab, F);
+    }
     for (int m = 0; m <= n_max; ++m) out[i * (n_max + 1) + m] = F[m];
 }
 
@@ -341,11 +346,14 @@ extern "C" int sq_boys_table(double *table64, float *table32, void *stream) {
     return check_launch("sq_boys_table");
 }
 
-extern "C" int sq_boys(int n_max, const double *z, long long nz, const double *table64, double *out, void *stream) {
-    if (!z || !table64 || !out || nz < 0) return set_error(SQ_ERR_ARG, "sq_boys: bad argument");
+extern "C" int sq_boys(int n_max, const double *z, long long nz, const double *table64, int mode, double *out,
+                       void *stream) {
+    if (!z || !table64 || !out || nz < 0 || (mode != 0 && mode != 1))
+        return set_error(SQ_ERR_ARG, "sq_boys: bad argument");
     if (n_max < 0 || n_max > SQ_BOYS_NCOL - 1 - kBoysTaylor64) return set_error(SQ_ERR_ARG, "sq_boys: n_max out of range");
     if (nz == 0) return SQ_OK;
-    boys_eval_kernel<<<(unsigned)((nz + 127) / 128), 128, 0, (cudaStream_t)stream>>>(n_max, z, nz, table64, out);
+    boys_eval_kernel<<<(unsigned)((nz + 127) / 128), 128, 0, (cudaStream_t)stream>>>(n_max, z, nz, table64, mode,
+                                                                                  out);
     return check_launch("sq_boys");
 }
 

@@ -35,24 +35,38 @@ def _lib_ready(gpu_lib):
     _lib.lib().sq_set_option(_lib.SQ_OPT_GENERIC_MIN_L, 5)
 
 
-def test_boys_against_oracle():
+def _gpu_boys(eng, z, nmax, mode):
     import torch
 
     from slowquant_gb300 import _lib
 
+    zt = torch.tensor(z, dtype=torch.float64, device="cuda")
+    out = torch.zeros((len(z), nmax + 1), dtype=torch.float64, device="cuda")
+    _lib.check(_lib.lib().sq_boys(nmax, zt.data_ptr(), len(z), eng.tab64.data_ptr(), mode, out.data_ptr(),
+                                  _lib.stream_handle()), "sq_boys")
+    return out.cpu().numpy()
+
+
+def _oracle_boys(z, nmax, mode):
+    O.lib().sqo_set_boys_mode(mode)
+    try:
+        return np.array([[O.boys(n, zz) for n in range(nmax + 1)] for zz in z])
+    finally:
+        O.lib().sqo_set_boys_mode(0)
+
+
+def test_boys_against_oracle():
+    """Tabulated Boys vs the exact series; reference-mode Boys vs the reference's formula."""
     eng = _engine("H 0 0 0;H 0 0 1.4", "sto-3g", "bohr")
     z = np.concatenate([[0.0, 1e-14, 1e-9, 1e-4], np.linspace(0.001, 60, 1777), [35.99, 36.0, 36.01, 100.0, 1e4]])
     nmax = 8
-    zt = torch.tensor(z, dtype=torch.float64, device="cuda")
-    out = torch.zeros((len(z), nmax + 1), dtype=torch.float64, device="cuda")
-    _lib.check(_lib.lib().sq_boys(nmax, zt.data_ptr(), len(z), eng.tab64.data_ptr(), out.data_ptr(),
-                                  _lib.stream_handle()), "sq_boys")
-    got = out.cpu().numpy()
-    ref = np.array([[O.boys(n, zz) for n in range(nmax + 1)] for zz in z])
-    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12)
-    # away from the reference's z > 25 asymptotic switch both are exact to ~1e-14 relative
-    sel = (z < 24.0) | (z > 45.0)
-    np.testing.assert_allclose(got[sel], ref[sel], rtol=2e-13, atol=1e-300)
+    exact = _oracle_boys(z, nmax, 1)
+    # T >= 36 drops the e^{-T} term of the upward recursion: < 1e-17 absolute
+    np.testing.assert_allclose(_gpu_boys(eng, z, nmax, 0), exact, rtol=2e-14, atol=1e-16)
+    ref = _oracle_boys(z, nmax, 0)
+    np.testing.assert_allclose(_gpu_boys(eng, z, nmax, 1), ref, rtol=1e-13, atol=1e-300)
+    # the reference's own truncation: large relative error for high n at small z
+    assert np.max(np.abs(ref - exact) / exact) > 1e-7
 
 
 @pytest.mark.parametrize("name", SYSTEMS)
