@@ -30,20 +30,22 @@ sys.path.insert(0, ROOT)
 
 METRIC = "ERI quartets/s & Fock-build ms, mixed vs FP64 plain on GPU at |ΔE|≤1e-6 Eh"
 WATERS, BOX, SEED, BASIS = 16, 11.0, 16, "cc-pvdz"
+BOXES = {16: 11.0, 8: 9.0}
 SCREEN, FP32_THR = 1e-12, 1e-4
 
 
 def workload_geometry() -> str:
     from slowquant_gb300 import systems
 
-    return systems.water_cluster(WATERS, BOX, SEED)
+    return systems.water_cluster(WATERS, BOXES.get(WATERS, BOX), SEED)
 
 
 def config(extra=None) -> dict:
     c = {
-        "workload": f"(H2O)_{WATERS} cc-pVDZ Fock build (J+K), 400 Cartesian bf, 11 A cube seed {SEED}",
+        "workload": f"(H2O)_{WATERS} cc-pVDZ Fock build (J+K), {25 * WATERS} Cartesian bf, "
+                    f"{BOXES.get(WATERS, BOX):g} A cube seed {SEED}",
         "molecule": f"(H2O)_{WATERS}",
-        "basis": "cc-pVDZ (Cartesian, 400 bf)",
+        "basis": f"cc-pVDZ (Cartesian, {25 * WATERS} bf)",
         "schwarz_threshold": SCREEN,
         "fp32_schwarz_threshold": FP32_THR,
         "precision": "mixed (FP32 quartets below bound 1e-4, FP64 Boys recursion; FP64 above)",
@@ -312,9 +314,13 @@ def gpu_arm(args) -> None:
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         t_wall = time.time()
+        torch.cuda.nvtx.range_push("timed_mixed")
         ms_mixed = time_events(torch, step_mixed, args.steps, flush)
+        torch.cuda.nvtx.range_pop()
         wall_mixed = time.time() - t_wall
+    torch.cuda.nvtx.range_push("timed_fp64")
     ms_fp64 = time_events(torch, step_fp64, max(3, min(args.steps, 5)), flush)
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     tot_mixed = sum(ms_mixed)
     if world > 1:
@@ -420,7 +426,11 @@ def main() -> None:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--waters", type=int, default=16, choices=[8, 16],
+                    help="cluster size (16 is the benchmark workload; 8 for quick profiling)")
     args = ap.parse_args()
+    global WATERS, SEED
+    WATERS = SEED = args.waters
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
