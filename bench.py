@@ -140,7 +140,8 @@ def class_work(eng, ql) -> dict:
 
     from slowquant_gb300 import flops
 
-    npp = torch.tensor(eng.pair_np, dtype=torch.int64, device=eng.device)
+    # quartet entries are slot ids: primitive pairs per slot
+    npp = torch.tensor(eng.pair_np[eng.slot_pair], dtype=torch.int64, device=eng.device)
     out = {}
     for c in range(21):
         a, b = int(ql.class_off[c]), int(ql.class_off[c + 1])
@@ -405,7 +406,7 @@ def gpu_arm(args) -> None:
         "hbm_peak_gbs": measured_peaks().get("hbm_gbs"),
     }
     if rank == 0 and not args.no_cpu:
-        pairs_host = (eng.pair_shells, q_all.pairs[: q_all.nquartet].cpu().numpy())
+        pairs_host = (eng.pair_shells[eng.slot_pair], q_all.pairs[: q_all.nquartet].cpu().numpy())
         rate, nthreads, n, dt = cpu_sample(None, args.cpu_seconds, 0, pairs_host, geom)
         line["cpu_baseline"] = {
             "value": rate, "unit": "quartets/s", "cores": nthreads, "kind": "port",

@@ -30,16 +30,25 @@ extern "C" {
 #define SQ_MAX_L 2            /* highest shell angular momentum (d) of the ERI kernels */
 #define SQ_MAX_QCLASS 21      /* quartet classes for l <= SQ_MAX_L: 6 pair classes -> 21 */
 
-/* Boys-function grid: F_m(T_k), T_k = k / SQ_BOYS_STEP_INV, k < SQ_BOYS_NGRID,
- * m < SQ_BOYS_NCOL - 1; column SQ_BOYS_NCOL-1 holds exp(-T_k). */
+/* Boys-function grid, T_k = k / SQ_BOYS_STEP_INV, k < SQ_BOYS_NGRID.
+ * FP64 table (SQ_BOYS_TAB64_SIZE doubles):
+ *   [0, NGRID*NCOL): F_m(T_k) at [k*NCOL + m], m < NCOL-1; column NCOL-1 = exp(-T_k);
+ *   [SQ_BOYS_TAY64_OFF, ...): Taylor coefficients F_{m+j}(T_k)/j! at
+ *     [(m*NGRID + k)*8 + j], j < 7, m < 15; block m = 15 holds exp(-T_k)/j!.
+ * FP32 table (SQ_BOYS_TAB32_SIZE floats): the same F grid, then
+ *   [SQ_BOYS_TAY32_OFF + (m*NGRID + k)*4 + j], j < 4. */
 #define SQ_BOYS_NGRID 580
 #define SQ_BOYS_STEP_INV 16
 #define SQ_BOYS_NCOL 16
 #define SQ_BOYS_TMAX 36.0
+#define SQ_BOYS_TAY64_OFF (SQ_BOYS_NGRID * SQ_BOYS_NCOL)
+#define SQ_BOYS_TAB64_SIZE (SQ_BOYS_TAY64_OFF + 16 * SQ_BOYS_NGRID * 8)
+#define SQ_BOYS_TAY32_OFF (SQ_BOYS_NGRID * SQ_BOYS_NCOL)
+#define SQ_BOYS_TAB32_SIZE (SQ_BOYS_TAY32_OFF + 16 * SQ_BOYS_NGRID * 4)
 
 /* Precision of one ERI / J-K launch. */
 #define SQ_FP64 0             /* all arithmetic in FP64 */
-#define SQ_FP32 1             /* FP32 integral arithmetic, FP64 Boys downward recursion */
+#define SQ_FP32 1             /* FP32 integral arithmetic, Boys downward recursion in FP64 */
 #define SQ_FP32_BOYS32 2      /* FP32 integral arithmetic and FP32 Boys function */
 
 /* Contracted Cartesian Gaussian shells of one molecule (device arrays).
@@ -76,6 +85,31 @@ typedef struct sq_pairs {
     float *herm32;             /* optional FP32 copy of herm */
 } sq_pairs;
 
+/* Slot layout of the pair data for the J/K kernels.  Pairs are renumbered in
+ * group order (a group = same pair class and primitive counts, sorted by
+ * descending Schwarz factor); slot s holds pair pair[s].  Primitive-pair data
+ * are stored field-major with the slots of one group fastest, so threads that
+ * work on consecutive slots of a group load consecutive addresses:
+ *   field f of primitive pair k of slot s: prim[f * npp_total + pbase[s] + k * pstride[s]]
+ *   Hermite value e of primitive pair k:   herm[hbase[s] + (k * E + e) * pstride[s]]
+ * (E = values per primitive pair of the slot's class, f < 5: p, Px, Py, Pz, U).
+ * The caller fills the index arrays and allocates the data arrays;
+ * sq_slots_fill copies them from sq_pairs. */
+typedef struct sq_slots {
+    int nslot;
+    long long npp_total;
+    long long nherm_total;
+    const int *pair;           /* [nslot] */
+    const int *npp;            /* [nslot] primitive pairs of the slot */
+    const int *pbase;          /* [nslot] */
+    const int *pstride;        /* [nslot] */
+    const long long *hbase;    /* [nslot] */
+    double *prim;              /* [5][npp_total] */
+    double *herm;              /* [nherm_total] */
+    float *prim32;             /* optional FP32 copies (NULL: not written) */
+    float *herm32;
+} sq_slots;
+
 /* Shell-quartet work list: device array of (bra pair, ket pair) index pairs,
  * grouped by quartet class; class_off (host) delimits each class segment.
  * Quartet class of pair classes cb >= ck is cb*(cb+1)/2 + ck. */
@@ -92,13 +126,15 @@ const char *sq_last_error(void);
 /* Process-wide tuning options (no reference counterpart).
  * SQ_OPT_GENERIC_MIN_L: quartet classes with la+lb+lc+ld >= value run on the
  * generic warp-cooperative kernel, the others on the per-class unrolled
- * kernels (default 5; 0 sends every class to the generic kernel). */
+ * kernels (default 5; SQ_FP32 launches of the classes up to (dd|ds) stay
+ * unrolled unless the value is 0, which sends every class to the generic
+ * kernel). */
 #define SQ_OPT_GENERIC_MIN_L 1
 int sq_set_option(int key, long long value);
 long long sq_get_option(int key);
 
-/* Fill the FP64 Boys grid table (SQ_BOYS_NGRID x SQ_BOYS_NCOL doubles) and,
- * if table32 != NULL, its FP32 copy.  Replaces nothing: the reference
+/* Fill the FP64 Boys table (SQ_BOYS_TAB64_SIZE doubles) and, if
+ * table32 != NULL, the FP32 table (SQ_BOYS_TAB32_SIZE floats).  Replaces nothing: the reference
  * evaluates boys_function by series on every call
  * (slowquant/molecularintegrals/integralfunctions.py:74-97). */
 int sq_boys_table(double *table64, float *table32, void *stream);
@@ -122,15 +158,20 @@ int sq_pair_prep(const sq_basis *basis, sq_pairs *pairs, void *stream);
 int sq_schwarz(const sq_basis *basis, const sq_pairs *pairs, const sq_quartets *diagonal, const double *table64,
                double *q, void *stream);
 
-/* Dense ERI tensor V[nbf^4] (C order) from the quartets of `quartets`, each
- * block scattered to its eight index permutations: the output of
- * electron_repulsion_integral_driver (electronrepulsion.py:11-104).  V must be
- * zeroed by the caller. */
-int sq_eri_dense(const sq_basis *basis, const sq_pairs *pairs, const sq_quartets *quartets,
+/* Copy the primitive-pair data of `pairs` into the slot layout.  Replaces
+ * nothing in the reference (it recomputes pair data per quartet,
+ * electronrepulsion.py:206-237). */
+int sq_slots_fill(const sq_basis *basis, const sq_pairs *pairs, sq_slots *slots, void *stream);
+
+/* Dense ERI tensor V[nbf^4] (C order) from the quartets of `quartets` (slot
+ * ids when slots != NULL, else pair ids), each block scattered to its eight
+ * index permutations: the output of electron_repulsion_integral_driver
+ * (electronrepulsion.py:11-104).  V must be zeroed by the caller. */
+int sq_eri_dense(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, const sq_quartets *quartets,
                  const double *table64, double *V, void *stream);
 
 /* Integral-direct Coulomb / exchange build: for the unique quartets of
- * `quartets`, accumulate into Jacc/Kacc ([nbf][nbf], FP64, caller zeroes)
+ * `quartets` (slot ids of `slots`), accumulate into Jacc/Kacc ([nbf][nbf], FP64, caller zeroes)
  * so that sym(Jacc) = J = einsum("pqrs,sr->pq", ERI, D) and
  * sym(Kacc) = K = einsum("psqr,sr->pq", ERI, D), the two einsums of
  * run_hartree_fock (slowquant/hartreefock/hartreefock_in_memory.py:55-56).
@@ -139,9 +180,9 @@ int sq_eri_dense(const sq_basis *basis, const sq_pairs *pairs, const sq_quartets
  * scratch of nbf*nbf floats that FP32 launches fill with (float)D (unused,
  * may be NULL, for SQ_FP64); FP32 launches need pairs->prim32/herm32 and
  * table32. */
-int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_quartets *quartets, const double *table64,
-          const float *table32, const double *D, float *D32, double *Jacc, double *Kacc, int precision,
-          void *stream);
+int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, const sq_quartets *quartets,
+          const double *table64, const float *table32, const double *D, float *D32, double *Jacc, double *Kacc,
+          int precision, void *stream);
 
 /* F = H + J - K/2 with J = (Jacc + Jacc^T)/2, K = (Kacc + Kacc^T)/2
  * (hartreefock_in_memory.py:57); J and K may be NULL. */
@@ -154,10 +195,11 @@ int sq_fock_build(int nbf, const double *H, const double *Jacc, const double *Ka
 int sq_one_electron(const sq_basis *basis, const double *table64, double *S, double *T, double *V,
                     void *stream);
 
-/* Expand per-bra-pair tasks into the flat quartet list: task i writes
- * (bra[i], ket_list[ket_start[i] + k]) for k < count[i] at out[offset[i] + k].
- * offset is the exclusive prefix sum of count.  Replaces the shell-quartet
- * loops and the Schwarz skip of electronrepulsion.py:32-49. */
+/* Expand per-bra tasks into the flat quartet list: task i writes
+ * (bra[i], ket_list[ket_start[i] + k]) for k < count[i] at out[offset[i] + k],
+ * or (bra[i], ket_start[i] + k) when ket_list is NULL (slot ids).  offset is
+ * the exclusive prefix sum of count.  Replaces the shell-quartet loops and the
+ * Schwarz skip of electronrepulsion.py:32-49. */
 int sq_quartets_expand(long long ntask, const int *bra, const int *ket_start, const int *count,
                        const long long *offset, const int *ket_list, int *out_pairs, long long nquartet,
                        void *stream);

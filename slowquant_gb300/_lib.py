@@ -20,6 +20,8 @@ SQ_BOYS_NGRID = 580
 SQ_BOYS_STEP_INV = 16
 SQ_BOYS_NCOL = 16
 SQ_BOYS_TMAX = 36.0
+SQ_BOYS_TAB64_SIZE = SQ_BOYS_NGRID * SQ_BOYS_NCOL + 16 * SQ_BOYS_NGRID * 8
+SQ_BOYS_TAB32_SIZE = SQ_BOYS_NGRID * SQ_BOYS_NCOL + 16 * SQ_BOYS_NGRID * 4
 SQ_FP64 = 0
 SQ_FP32 = 1
 SQ_FP32_BOYS32 = 2
@@ -42,6 +44,14 @@ class SqPairs(ctypes.Structure):
     _fields_ = [
         ("npair", ctypes.c_int), ("nprimpair", ctypes.c_int), ("shells", _p), ("pp_off", _p),
         ("herm_off", _p), ("prim", _p), ("herm", _p), ("prim32", _p), ("herm32", _p),
+    ]
+
+
+class SqSlots(ctypes.Structure):
+    _fields_ = [
+        ("nslot", ctypes.c_int), ("npp_total", ctypes.c_longlong), ("nherm_total", ctypes.c_longlong),
+        ("pair", _p), ("npp", _p), ("pbase", _p), ("pstride", _p), ("hbase", _p),
+        ("prim", _p), ("herm", _p), ("prim32", _p), ("herm32", _p),
     ]
 
 
@@ -75,10 +85,11 @@ def lib() -> ctypes.CDLL:
         L.sq_pair_prep.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), _p]
         L.sq_schwarz.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqQuartets), _p,
                                  _p, _p]
-        L.sq_eri_dense.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqQuartets),
-                                   _p, _p, _p]
-        L.sq_jk.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqQuartets), _p, _p,
-                            _p, _p, _p, _p, ctypes.c_int, _p]
+        L.sq_eri_dense.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
+                                   ctypes.POINTER(SqQuartets), _p, _p, _p]
+        L.sq_jk.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
+                            ctypes.POINTER(SqQuartets), _p, _p, _p, _p, _p, _p, ctypes.c_int, _p]
+        L.sq_slots_fill.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots), _p]
         L.sq_fock_build.argtypes = [ctypes.c_int, _p, _p, _p, _p, _p, _p, _p]
         L.sq_one_electron.argtypes = [ctypes.POINTER(SqBasis), _p, _p, _p, _p, _p]
         L.sq_quartets_expand.argtypes = [ctypes.c_longlong, _p, _p, _p, _p, _p, _p, ctypes.c_longlong, _p]
@@ -90,7 +101,7 @@ def lib() -> ctypes.CDLL:
 EXPORTED = [
     "sq_version", "sq_last_error", "sq_set_option", "sq_get_option", "sq_boys_table", "sq_boys",
     "sq_pair_prep", "sq_schwarz", "sq_eri_dense", "sq_jk", "sq_fock_build", "sq_one_electron",
-    "sq_quartets_expand", "sq_fma_probe",
+    "sq_quartets_expand", "sq_fma_probe", "sq_slots_fill",
 ]
 
 

@@ -4,9 +4,11 @@
 // & Pople, Int. J. Quantum Chem. 40, 745 (1991)):
 //   * a grid T_k = k/16 (k < SQ_BOYS_NGRID) holds F_m(T_k) for m < 15 and
 //     exp(-T_k), built once by the series F_m(T) = e^{-T} sum_i (2T)^i /
-//     ((2m+1)(2m+3)...(2m+2i+1)) with compensated summation;
-//   * for T < 36, F_m(T) = sum_j F_{m+j}(T_k) (-d)^j / j!, d = T - T_k,
-//     |d| <= 1/32 (7 terms in FP64: truncation < 6e-15 relative; 4 in FP32);
+//     ((2m+1)(2m+3)...(2m+2i+1)) with compensated summation, and the scaled
+//     Taylor coefficients F_{m+j}(T_k)/j!, exp(-T_k)/j!;
+//   * for T < 36, F_m(T) = sum_j [F_{m+j}(T_k)/j!] (-d)^j, d = T - T_k,
+//     |d| <= 1/32 (7 terms in FP64: truncation < 6e-15 relative; 4 in FP32),
+//     a Horner chain of FMAs only;
 //     for m_max >= 2 only F_{m_max} is expanded and the lower orders follow
 //     from the stable downward recursion (2m+1) F_m = 2T F_{m+1} + e^{-T},
 //     with e^{-T} = e^{-T_k} e^{-d} from the same grid;
@@ -28,35 +30,49 @@ constexpr int kBoysTaylor64 = 7;
 constexpr int kBoysTaylor32 = 4;
 constexpr double kSqrtPiHalf = 0.88622692545275801365;  // sqrt(pi)/2
 
-// FP64: F[0..M] at T >= 0.  tab: SQ_BOYS_NGRID x SQ_BOYS_NCOL doubles.
+// Grid point of T (T >= 0, T < 36) computed on the FP32 / integer pipes, and
+// d = T - k/16 exactly: k/16 is built from the bit pattern of 2^48 + k/16
+// (a double with ulp 2^-4), so no FP64 conversion instruction is needed.
+__device__ __forceinline__ double boys_offset(double T, float Tf, int &k) {
+    k = __float2int_rn(Tf * (float)SQ_BOYS_STEP_INV);
+    const double kd16 = __longlong_as_double(0x42F0000000000000LL + (long long)k) - 281474976710656.0;
+    return T - kd16;
+}
+
+// Horner sum_j c[j] x^j of the 7 scaled Taylor coefficients of one grid row.
+__device__ __forceinline__ double taylor7(const double *__restrict__ row, double x) {
+    const double2 c01 = __ldg(reinterpret_cast<const double2 *>(row));
+    const double2 c23 = __ldg(reinterpret_cast<const double2 *>(row + 2));
+    const double2 c45 = __ldg(reinterpret_cast<const double2 *>(row + 4));
+    const double c6 = __ldg(row + 6);
+    double f = fma(c6, x, c45.y);
+    f = fma(f, x, c45.x);
+    f = fma(f, x, c23.y);
+    f = fma(f, x, c23.x);
+    f = fma(f, x, c01.y);
+    return fma(f, x, c01.x);
+}
+
+__device__ __forceinline__ float taylor4(const float *__restrict__ row, float x) {
+    const float4 c = __ldg(reinterpret_cast<const float4 *>(row));
+    return fmaf(fmaf(fmaf(c.w, x, c.z), x, c.y), x, c.x);
+}
+
+// FP64: F[0..M] at T >= 0.  tab: the FP64 table (SQ_BOYS_TAB64_SIZE doubles).
 template <int M>
 __device__ __forceinline__ void boys64(double T, const double *__restrict__ tab, double (&F)[M + 1]) {
     static_assert(M + kBoysTaylor64 <= SQ_BOYS_NCOL - 1, "Boys table too narrow for this order");
-    if (T < SQ_BOYS_TMAX) {
-        const int k = __double2int_rn(T * SQ_BOYS_STEP_INV);
-        const double d = T - k * (1.0 / SQ_BOYS_STEP_INV);
-        const double *row = tab + k * SQ_BOYS_NCOL;
-        // md[j] = -d / j
-        double md[kBoysTaylor64];
-#pragma unroll
-        for (int j = 1; j < kBoysTaylor64; ++j) md[j] = -d * (1.0 / j);
+    const float Tf = d2f_bits(T);
+    if (Tf < (float)SQ_BOYS_TMAX) {
+        int k;
+        const double md = -boys_offset(T, Tf, k);
+        const double *tay = tab + SQ_BOYS_TAY64_OFF + k * 8;
         if constexpr (M <= 1) {
 #pragma unroll
-            for (int m = 0; m <= M; ++m) {
-                double f = __ldg(row + m + kBoysTaylor64 - 1);
-#pragma unroll
-                for (int j = kBoysTaylor64 - 1; j >= 1; --j) f = fma(f, md[j], __ldg(row + m + j - 1));
-                F[m] = f;
-            }
+            for (int m = 0; m <= M; ++m) F[m] = taylor7(tay + m * SQ_BOYS_NGRID * 8, md);
         } else {
-            double f = __ldg(row + M + kBoysTaylor64 - 1);
-#pragma unroll
-            for (int j = kBoysTaylor64 - 1; j >= 1; --j) f = fma(f, md[j], __ldg(row + M + j - 1));
-            F[M] = f;
-            double e = 1.0;
-#pragma unroll
-            for (int j = kBoysTaylor64 - 1; j >= 1; --j) e = fma(e, md[j], 1.0);
-            e *= __ldg(row + SQ_BOYS_NCOL - 1);
+            F[M] = taylor7(tay + M * SQ_BOYS_NGRID * 8, md);
+            const double e = taylor7(tay + 15 * SQ_BOYS_NGRID * 8, md);
             const double T2 = T + T;
 #pragma unroll
             for (int m = M - 1; m >= 0; --m) F[m] = fma(T2, F[m + 1], e) * (1.0 / (2 * m + 1));
@@ -72,33 +88,23 @@ __device__ __forceinline__ void boys64(double T, const double *__restrict__ tab,
     }
 }
 
-// FP32 Boys from the FP32 copy of the grid.
+// FP32 Boys from two blocks of the FP32 Taylor table (rows of 4 floats per
+// grid point; global or shared memory): for M <= 1, b0/b1 are the blocks of
+// orders 0 and 1; for M >= 2, b0 is the block of order M and b1 the exp block.
+// 4-term Taylor, truncation < 4e-8 relative.
 template <int M>
-__device__ __forceinline__ void boys32(float T, const float *__restrict__ tab, float (&F)[M + 1]) {
+__device__ __forceinline__ void boys32(float T, const float4 *b0, const float4 *b1, float (&F)[M + 1]) {
     if (T < (float)SQ_BOYS_TMAX) {
         const int k = __float2int_rn(T * (float)SQ_BOYS_STEP_INV);
-        const float d = T - k * (1.0f / SQ_BOYS_STEP_INV);
-        const float *row = tab + k * SQ_BOYS_NCOL;
-        float md[kBoysTaylor32];
-#pragma unroll
-        for (int j = 1; j < kBoysTaylor32; ++j) md[j] = -d * (1.0f / j);
-        if constexpr (M <= 1) {
-#pragma unroll
-            for (int m = 0; m <= M; ++m) {
-                float f = __ldg(row + m + kBoysTaylor32 - 1);
-#pragma unroll
-                for (int j = kBoysTaylor32 - 1; j >= 1; --j) f = fmaf(f, md[j], __ldg(row + m + j - 1));
-                F[m] = f;
-            }
-        } else {
-            float f = __ldg(row + M + kBoysTaylor32 - 1);
-#pragma unroll
-            for (int j = kBoysTaylor32 - 1; j >= 1; --j) f = fmaf(f, md[j], __ldg(row + M + j - 1));
-            F[M] = f;
-            float e = 1.0f;
-#pragma unroll
-            for (int j = kBoysTaylor32 - 1; j >= 1; --j) e = fmaf(e, md[j], 1.0f);
-            e *= __ldg(row + SQ_BOYS_NCOL - 1);
+        const float md = k * (1.0f / SQ_BOYS_STEP_INV) - T;
+        const float4 c0 = b0[k];
+        F[M <= 1 ? 0 : M] = fmaf(fmaf(fmaf(c0.w, md, c0.z), md, c0.y), md, c0.x);
+        if constexpr (M == 1) {
+            const float4 c1 = b1[k];
+            F[1] = fmaf(fmaf(fmaf(c1.w, md, c1.z), md, c1.y), md, c1.x);
+        } else if constexpr (M >= 2) {
+            const float4 ce = b1[k];
+            const float e = fmaf(fmaf(fmaf(ce.w, md, ce.z), md, ce.y), md, ce.x);
             const float T2 = T + T;
 #pragma unroll
             for (int m = M - 1; m >= 0; --m) F[m] = fmaf(T2, F[m + 1], e) * (1.0f / (2 * m + 1));
@@ -112,6 +118,41 @@ __device__ __forceinline__ void boys32(float T, const float *__restrict__ tab, f
             for (int m = 0; m < M; ++m) F[m + 1] = F[m] * ((2 * m + 1) * h);
         }
     }
+}
+
+// Mixed Boys for FP32 quartets: F_M and e^{-T} from the FP32 table (Taylor,
+// FP32), then the downward recursion (2m+1) F_m = 2T F_{m+1} + e^{-T} in FP64;
+// the results are handed back as FP32.  M <= 1 needs no recursion (each order
+// has its own FP32 expansion), so those classes stay entirely in FP32.
+template <int M>
+__device__ __forceinline__ void boys_mixed(float T, const float4 *b0, const float4 *b1, float (&F)[M + 1]) {
+    if constexpr (M <= 1) {
+        boys32<M>(T, b0, b1, F);
+    } else {
+        if (T < (float)SQ_BOYS_TMAX) {
+            const int k = __float2int_rn(T * (float)SQ_BOYS_STEP_INV);
+            const float md = k * (1.0f / SQ_BOYS_STEP_INV) - T;
+            const float4 c0 = b0[k], ce = b1[k];
+            const float f = fmaf(fmaf(fmaf(c0.w, md, c0.z), md, c0.y), md, c0.x);
+            const float e = fmaf(fmaf(fmaf(ce.w, md, ce.z), md, ce.y), md, ce.x);
+            F[M] = f;
+            const double T2 = f2d_bits(T + T), ed = f2d_bits(e);
+            double fd = f2d_bits(f);
+#pragma unroll
+            for (int m = M - 1; m >= 0; --m) {
+                fd = fma(T2, fd, ed) * (1.0 / (2 * m + 1));
+                F[m] = d2f_bits(fd);
+            }
+        } else {
+            boys32<M>(T, b0, b1, F);
+        }
+    }
+}
+
+// Blocks of the FP32 Taylor table used by an order-M evaluation.
+template <int M>
+__host__ __device__ constexpr int boys32_block(int which) {
+    return M <= 1 ? which : (which == 0 ? M : 15);
 }
 
 // Runtime-order FP64 Boys (used by the one-electron kernel and the test hook):

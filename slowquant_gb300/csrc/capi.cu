@@ -27,10 +27,21 @@ int check_launch(const char *what) {
 #define DECL(QC) cudaError_t launch_qc_##QC(const EriArgs &, int, int, cudaStream_t);
 DECL(0) DECL(1) DECL(2) DECL(3) DECL(4) DECL(5) DECL(6) DECL(7) DECL(8) DECL(9) DECL(10) DECL(11)
 #undef DECL
+#define DECL32(QC) cudaError_t launch_qc_##QC##_f32(const EriArgs &, int, int, cudaStream_t);
+DECL32(12) DECL32(13) DECL32(14) DECL32(15) DECL32(16) DECL32(17) DECL32(18)
+#undef DECL32
+
+// FP32 (SQ_FP32) per-thread kernels of the heavy classes.
+static const eri_launcher kLaunchersF32[SQ_MAX_QCLASS] = {
+    nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+    nullptr, nullptr, nullptr, nullptr, nullptr, launch_qc_12_f32, launch_qc_13_f32,
+    launch_qc_14_f32, launch_qc_15_f32, launch_qc_16_f32, launch_qc_17_f32, launch_qc_18_f32, nullptr, nullptr,
+};
 
 // Per-thread (fully unrolled) J/K kernels exist for the light classes (L <= 4,
-// except (dd|ss)); every other class, and every dense-tensor or Schwarz launch,
-// runs on the generic warp kernel.
+// except (dd|ss)) in every precision, and for classes 12-18 in SQ_FP32; every
+// other class/precision, and every dense-tensor or Schwarz launch, runs on the
+// generic warp kernel.  SQ_OPT_GENERIC_MIN_L = 0 sends everything to it.
 static const eri_launcher kLaunchers[SQ_MAX_QCLASS] = {
     launch_qc_0, launch_qc_1, launch_qc_2, launch_qc_3, launch_qc_4, launch_qc_5, launch_qc_6,
     launch_qc_7, launch_qc_8, launch_qc_9, launch_qc_10, launch_qc_11, nullptr, nullptr,
@@ -79,10 +90,16 @@ static int run_classes(const char *who, EriArgs args, const sq_quartets *qs, int
         int la, lb, lc, ld;
         quartet_class_l(c, la, lb, lc, ld);
         cudaError_t e;
-        if (mode != MODE_JK || la + lb + lc + ld >= g_generic_min_l || kLaunchers[c] == nullptr)
-            e = launch_eri_warp(args, WarpClass{la, lb, lc, ld}, mode, precision, stream);
+        const int L = la + lb + lc + ld;
+        eri_launcher unrolled = nullptr;
+        if (mode == MODE_JK && L < g_generic_min_l) unrolled = kLaunchers[c];
+        if (mode == MODE_JK && precision == SQ_FP32 && kLaunchersF32[c] != nullptr &&
+            g_generic_min_l > 0)
+            unrolled = kLaunchersF32[c];
+        if (unrolled != nullptr)
+            e = unrolled(args, mode, precision, stream);
         else
-            e = kLaunchers[c](args, mode, precision, stream);
+            e = launch_eri_warp(args, WarpClass{la, lb, lc, ld}, mode, precision, stream);
         if (e != cudaSuccess) return set_error(SQ_ERR_CUDA, "%s: class %d: %s", who, c, cudaGetErrorString(e));
     }
     return SQ_OK;
@@ -123,31 +140,37 @@ extern "C" int sq_schwarz(const sq_basis *basis, const sq_pairs *pairs, const sq
     return run_classes("sq_schwarz", a, diagonal, MODE_SCHWARZ, SQ_FP64, (cudaStream_t)stream);
 }
 
-extern "C" int sq_eri_dense(const sq_basis *basis, const sq_pairs *pairs, const sq_quartets *quartets,
-                            const double *table64, double *V, void *stream) {
+extern "C" int sq_eri_dense(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots,
+                            const sq_quartets *quartets, const double *table64, double *V, void *stream) {
     int rc = check_common("sq_eri_dense", basis, pairs, quartets, table64);
     if (rc) return rc;
     if (!V) return set_error(SQ_ERR_ARG, "sq_eri_dense: V is NULL");
     EriArgs a{};
     a.basis = *basis;
     a.pairs = *pairs;
+    if (slots) {
+        a.slots = *slots;
+        a.use_slots = 1;
+    }
     a.tab64 = table64;
     a.V = V;
     return run_classes("sq_eri_dense", a, quartets, MODE_DENSE, SQ_FP64, (cudaStream_t)stream);
 }
 
-extern "C" int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_quartets *quartets,
-                     const double *table64, const float *table32, const double *D, float *D32, double *Jacc,
-                     double *Kacc, int precision, void *stream) {
+extern "C" int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots,
+                     const sq_quartets *quartets, const double *table64, const float *table32, const double *D,
+                     float *D32, double *Jacc, double *Kacc, int precision, void *stream) {
     int rc = check_common("sq_jk", basis, pairs, quartets, table64);
     if (rc) return rc;
+    if (!slots || !slots->prim || !slots->herm || !slots->pair)
+        return set_error(SQ_ERR_ARG, "sq_jk: slot layout is required");
     if (!D || !Jacc || !Kacc) return set_error(SQ_ERR_ARG, "sq_jk: D, Jacc and Kacc are required");
     if (precision != SQ_FP64 && precision != SQ_FP32 && precision != SQ_FP32_BOYS32)
         return set_error(SQ_ERR_ARG, "sq_jk: unknown precision %d", precision);
     cudaStream_t s = (cudaStream_t)stream;
     if (precision != SQ_FP64) {
-        if (!D32 || !pairs->prim32 || !pairs->herm32 || (precision == SQ_FP32_BOYS32 && !table32))
-            return set_error(SQ_ERR_ARG, "sq_jk: FP32 precision needs D32, prim32, herm32 and table32");
+        if (!D32 || !pairs->prim32 || !pairs->herm32 || !slots->prim32 || !slots->herm32 || !table32)
+            return set_error(SQ_ERR_ARG, "sq_jk: FP32 precision needs D32, FP32 pair/slot data and table32");
         rc = to_float((long long)basis->nbf * basis->nbf, D, D32, s);
         if (rc) return rc;
     }
@@ -158,6 +181,8 @@ extern "C" int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_quar
     a.tab32 = table32;
     a.D = D;
     a.D32 = D32;
+    a.slots = *slots;
+    a.use_slots = 1;
     a.Jacc = Jacc;
     a.Kacc = Kacc;
     return run_classes("sq_jk", a, quartets, MODE_JK, precision, s);

@@ -34,6 +34,8 @@ enum { BOYS_FP64 = 0, BOYS_FP32 = 1, BOYS_REF = 2 };
 struct EriArgs {
     sq_basis basis;
     sq_pairs pairs;
+    sq_slots slots;   // J/K and dense lists hold slot ids
+    int use_slots;    // 0: quartet entries are pair ids (Schwarz lists)
     const int2 *quartets;
     long long nq;
     const double *tab64;
@@ -61,6 +63,21 @@ __device__ __forceinline__ const R *prim_ptr(const sq_pairs &pr) {
         return pr.prim;
     else
         return pr.prim32;
+}
+
+template <typename R>
+__device__ __forceinline__ const R *slot_prim_ptr(const sq_slots &sl) {
+    if constexpr (std::is_same<R, double>::value)
+        return sl.prim;
+    else
+        return sl.prim32;
+}
+template <typename R>
+__device__ __forceinline__ const R *slot_herm_ptr(const sq_slots &sl) {
+    if constexpr (std::is_same<R, double>::value)
+        return sl.herm;
+    else
+        return sl.herm32;
 }
 
 template <typename R>
@@ -122,31 +139,42 @@ __device__ __forceinline__ T gload(const T *p) {
 }
 
 // Contracted block of one quartet: acc[a*NB+b][c*ND+d].
+//
+// FP64 work per primitive quartet is what bounds these kernels on GB300, so:
+// the bra factor 2 pi^{5/2} U_bra is applied once per bra primitive pair (in
+// the bra transform), the Hermite coefficients of s-s pairs (exactly 1) are
+// neither loaded nor multiplied, and (ss|ss) accumulates with a single FMA.
 template <int LA, int LB, int LC, int LD, typename R, int BOYS>
-__device__ __forceinline__ void quartet_block(const EriArgs &args, int P, int Q,
+__device__ __forceinline__ void quartet_block(const EriArgs &args, int P, int Q, const float4 *tb0,
+                                              const float4 *tb1,
                                               R (&acc)[ncart(LA) * ncart(LB)][ncart(LC) * ncart(LD)]) {
     constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
     constexpr int NAB = NA * NB, NCD = NC * ND;
     constexpr int LAB = LA + LB, LCD = LC + LD, L = LAB + LCD;
     constexpr int EB = herm_size(LA, LB), EK = herm_size(LC, LD);
+    constexpr bool BRA_S = (LAB == 0), KET_S = (LCD == 0);
 
-    const sq_pairs &pr = args.pairs;
-    const R *prim = prim_ptr<R>(pr);
-    const R *herm = herm_ptr<R>(pr);
-    const int i0 = gload(pr.pp_off + P), i1 = gload(pr.pp_off + P + 1);
-    const int k0 = gload(pr.pp_off + Q), k1 = gload(pr.pp_off + Q + 1);
-    const R *hb = herm + gload(pr.herm_off + P);
-    const R *hk = herm + gload(pr.herm_off + Q);
+    // slot layout: field f of primitive pair i of slot s at prim[f*NPP + pbase[s] + i*pstride[s]]
+    const sq_slots &sl = args.slots;
+    const R *prim = slot_prim_ptr<R>(sl);
+    const R *herm = slot_herm_ptr<R>(sl);
+    const long long NPP = sl.npp_total;
+    const int nb = gload(sl.npp + P), nk = gload(sl.npp + Q);
+    const int pb = gload(sl.pbase + P), sb = gload(sl.pstride + P);
+    const int pk = gload(sl.pbase + Q), sk = gload(sl.pstride + Q);
+    const R *hb = herm + gload(sl.hbase + P);
+    const R *hk = herm + gload(sl.hbase + Q);
 
 #pragma unroll
     for (int x = 0; x < NAB; ++x)
 #pragma unroll
         for (int y = 0; y < NCD; ++y) acc[x][y] = R(0);
 
-    for (int i = i0; i < i1; ++i) {
-        const R p = gload(prim + 8 * i + 0);
-        const R Px = gload(prim + 8 * i + 1), Py = gload(prim + 8 * i + 2), Pz = gload(prim + 8 * i + 3);
-        const R Ub = gload(prim + 8 * i + 4);
+    for (int i = 0; i < nb; ++i) {
+        const long long ib = pb + (long long)i * sb;
+        const R p = gload(prim + ib);
+        const R Px = gload(prim + NPP + ib), Py = gload(prim + 2 * NPP + ib), Pz = gload(prim + 3 * NPP + ib);
+        const R Ub = gload(prim + 4 * NPP + ib);
         R W[LAB + 1][LAB + 1][LAB + 1][NCD];
 #pragma unroll
         for (int t = 0; t <= LAB; ++t)
@@ -157,92 +185,104 @@ __device__ __forceinline__ void quartet_block(const EriArgs &args, int P, int Q,
 #pragma unroll
                     for (int y = 0; y < NCD; ++y) W[t][u][v][y] = R(0);
 
-        for (int k = k0; k < k1; ++k) {
-            const R q = gload(prim + 8 * k + 0);
-            const R X = Px - gload(prim + 8 * k + 1);
-            const R Y = Py - gload(prim + 8 * k + 2);
-            const R Z = Pz - gload(prim + 8 * k + 3);
-            const R Uk = gload(prim + 8 * k + 4);
+        for (int k = 0; k < nk; ++k) {
+            const long long ik = pk + (long long)k * sk;
+            const R q = gload(prim + ik);
+            const R X = Px - gload(prim + NPP + ik);
+            const R Y = Py - gload(prim + 2 * NPP + ik);
+            const R Z = Pz - gload(prim + 3 * NPP + ik);
+            const R Uk = gload(prim + 4 * NPP + ik);
             const R r = rsqrt_r(p + q);
             const R alpha = p * q * (r * r);
             const R T = alpha * (X * X + Y * Y + Z * Z);
-            R Fs[L + 1];
+            R F[L + 1];
             if constexpr (std::is_same<R, double>::value) {
-                double F[L + 1];
                 boys64<L>(T, args.tab64, F);
-#pragma unroll
-                for (int n = 0; n <= L; ++n) Fs[n] = F[n];
             } else if constexpr (BOYS == BOYS_FP64) {
-                double F[L + 1];
-                boys64<L>((double)T, args.tab64, F);
-#pragma unroll
-                for (int n = 0; n <= L; ++n) Fs[n] = (R)F[n];
+                boys_mixed<L>(T, tb0, tb1, F);
             } else {
-                float F[L + 1];
-                boys32<L>(T, args.tab32, F);
-#pragma unroll
-                for (int n = 0; n <= L; ++n) Fs[n] = F[n];
+                boys32<L>(T, tb0, tb1, F);
             }
-            R fac = R(kTwoPi52) * Ub * Uk * r;
-            const R m2a = R(-2) * alpha;
+            R fac = Uk * r;
+            if constexpr (L == 0) {
+                W[0][0][0][0] = fma(F[0], fac, W[0][0][0][0]);
+            } else {
+                R Fs[L + 1];
+                const R m2a = R(-2) * alpha;
 #pragma unroll
-            for (int n = 0; n <= L; ++n) {
-                Fs[n] *= fac;
-                fac *= m2a;
+                for (int n = 0; n <= L; ++n) {
+                    Fs[n] = F[n] * fac;
+                    if (n < L) fac *= m2a;
+                }
+                R Rt[L + 1][L + 1][L + 1];
+                hermite_r<L, R>(Fs, X, Y, Z, Rt);
+                if constexpr (KET_S) {
+#pragma unroll
+                    for (int t = 0; t <= LAB; ++t)
+#pragma unroll
+                        for (int u = 0; u <= LAB - t; ++u)
+#pragma unroll
+                            for (int v = 0; v <= LAB - t - u; ++v) W[t][u][v][0] += Rt[t][u][v];
+                } else {
+                    // W[tuv][cd] += sum_{tau nu phi} (-1)^{tau+nu+phi} E^{cd}_{tau nu phi} R[t+tau][u+nu][v+phi]
+                    const R *ek = hk + (long long)k * EK * sk;
+#pragma unroll
+                    for (int c = 0; c < NC; ++c)
+#pragma unroll
+                        for (int d = 0; d < ND; ++d) {
+                            const int cx = cart_x(LC, c) + cart_x(LD, d);
+                            const int cy = cart_y(LC, c) + cart_y(LD, d);
+                            const int cz = cart_z(LC, c) + cart_z(LD, d);
+                            const int off = herm_offset(LC, LD, c, d);
+#pragma unroll
+                            for (int tau = 0; tau <= cx; ++tau)
+#pragma unroll
+                                for (int nu = 0; nu <= cy; ++nu)
+#pragma unroll
+                                    for (int phi = 0; phi <= cz; ++phi) {
+                                        R e = gload(ek + (long long)(off + (tau * (cy + 1) + nu) * (cz + 1) + phi) * sk);
+                                        if ((tau + nu + phi) & 1) e = -e;
+#pragma unroll
+                                        for (int t = 0; t <= LAB; ++t)
+#pragma unroll
+                                            for (int u = 0; u <= LAB - t; ++u)
+#pragma unroll
+                                                for (int v = 0; v <= LAB - t - u; ++v)
+                                                    W[t][u][v][c * ND + d] =
+                                                        fma(e, Rt[t + tau][u + nu][v + phi], W[t][u][v][c * ND + d]);
+                                    }
+                        }
+                }
             }
-            R Rt[L + 1][L + 1][L + 1];
-            hermite_r<L, R>(Fs, X, Y, Z, Rt);
-
-            // ket transform: W[tuv][cd] += sum_{tau nu phi} (-1)^{tau+nu+phi} E^{cd}_{tau nu phi} R[t+tau][u+nu][v+phi]
-            const R *ek = hk + (k - k0) * EK;
+        }
+        // bra transform with the bra factor 2 pi^{5/2} U_bra
+        const R ub = R(kTwoPi52) * Ub;
+        if constexpr (BRA_S) {
 #pragma unroll
-            for (int c = 0; c < NC; ++c)
+            for (int y = 0; y < NCD; ++y) acc[0][y] = fma(ub, W[0][0][0][y], acc[0][y]);
+        } else {
+            const R *eb = hb + (long long)i * EB * sb;
 #pragma unroll
-                for (int d = 0; d < ND; ++d) {
-                    const int cx = cart_x(LC, c) + cart_x(LD, d);
-                    const int cy = cart_y(LC, c) + cart_y(LD, d);
-                    const int cz = cart_z(LC, c) + cart_z(LD, d);
-                    const int off = herm_offset(LC, LD, c, d);
+            for (int a = 0; a < NA; ++a)
 #pragma unroll
-                    for (int tau = 0; tau <= cx; ++tau)
+                for (int b = 0; b < NB; ++b) {
+                    const int ax = cart_x(LA, a) + cart_x(LB, b);
+                    const int ay = cart_y(LA, a) + cart_y(LB, b);
+                    const int az = cart_z(LA, a) + cart_z(LB, b);
+                    const int off = herm_offset(LA, LB, a, b);
 #pragma unroll
-                        for (int nu = 0; nu <= cy; ++nu)
+                    for (int t = 0; t <= ax; ++t)
 #pragma unroll
-                            for (int phi = 0; phi <= cz; ++phi) {
-                                R e = gload(ek + off + (tau * (cy + 1) + nu) * (cz + 1) + phi);
-                                if ((tau + nu + phi) & 1) e = -e;
+                        for (int u = 0; u <= ay; ++u)
 #pragma unroll
-                                for (int t = 0; t <= LAB; ++t)
+                            for (int v = 0; v <= az; ++v) {
+                                const R e = ub * gload(eb + (long long)(off + (t * (ay + 1) + u) * (az + 1) + v) * sb);
 #pragma unroll
-                                    for (int u = 0; u <= LAB - t; ++u)
-#pragma unroll
-                                        for (int v = 0; v <= LAB - t - u; ++v)
-                                            W[t][u][v][c * ND + d] =
-                                                fma(e, Rt[t + tau][u + nu][v + phi], W[t][u][v][c * ND + d]);
+                                for (int y = 0; y < NCD; ++y)
+                                    acc[a * NB + b][y] = fma(e, W[t][u][v][y], acc[a * NB + b][y]);
                             }
                 }
         }
-        // bra transform
-        const R *eb = hb + (i - i0) * EB;
-#pragma unroll
-        for (int a = 0; a < NA; ++a)
-#pragma unroll
-            for (int b = 0; b < NB; ++b) {
-                const int ax = cart_x(LA, a) + cart_x(LB, b);
-                const int ay = cart_y(LA, a) + cart_y(LB, b);
-                const int az = cart_z(LA, a) + cart_z(LB, b);
-                const int off = herm_offset(LA, LB, a, b);
-#pragma unroll
-                for (int t = 0; t <= ax; ++t)
-#pragma unroll
-                    for (int u = 0; u <= ay; ++u)
-#pragma unroll
-                        for (int v = 0; v <= az; ++v) {
-                            const R e = gload(eb + off + (t * (ay + 1) + u) * (az + 1) + v);
-#pragma unroll
-                            for (int y = 0; y < NCD; ++y) acc[a * NB + b][y] = fma(e, W[t][u][v][y], acc[a * NB + b][y]);
-                        }
-            }
     }
 }
 
@@ -250,15 +290,32 @@ template <int LA, int LB, int LC, int LD, typename R, int BOYS, int MODE>
 __global__ void __launch_bounds__(128) eri_class_kernel(const EriArgs args) {
     constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
     constexpr int NAB = NA * NB, NCD = NC * ND;
+    constexpr int L = LA + LB + LC + LD;
+    // FP32 launches read the two Boys Taylor blocks they need from shared memory
+    // (random rows: one smem wavefront per 8 lanes instead of one L1 sector per lane).
+    __shared__ float4 s_tab[std::is_same<R, float>::value ? 2 : 1][std::is_same<R, float>::value ? SQ_BOYS_NGRID : 1];
+    const float4 *tb0 = nullptr, *tb1 = nullptr;
+    if constexpr (std::is_same<R, float>::value) {
+        const float4 *g = reinterpret_cast<const float4 *>(args.tab32 + SQ_BOYS_TAY32_OFF);
+        const int blk0 = boys32_block<L>(0), blk1 = boys32_block<L>(1);
+        for (int x = threadIdx.x; x < SQ_BOYS_NGRID; x += blockDim.x) {
+            s_tab[0][x] = g[blk0 * SQ_BOYS_NGRID + x];
+            s_tab[1][x] = g[blk1 * SQ_BOYS_NGRID + x];
+        }
+        __syncthreads();
+        tb0 = s_tab[0];
+        tb1 = s_tab[1];
+    }
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long qi = (long long)blockIdx.x * blockDim.x + threadIdx.x; qi < args.nq; qi += stride) {
         const int2 pq = args.quartets[qi];
         const int P = pq.x, Q = pq.y;
         R acc[NAB][NCD];
-        quartet_block<LA, LB, LC, LD, R, BOYS>(args, P, Q, acc);
+        quartet_block<LA, LB, LC, LD, R, BOYS>(args, P, Q, tb0, tb1, acc);
 
-        const int sa = gload(args.pairs.shells + 2 * P), sb = gload(args.pairs.shells + 2 * P + 1);
-        const int sc = gload(args.pairs.shells + 2 * Q), sd = gload(args.pairs.shells + 2 * Q + 1);
+        const int pairP = gload(args.slots.pair + P), pairQ = gload(args.slots.pair + Q);
+        const int sa = gload(args.pairs.shells + 2 * pairP), sb = gload(args.pairs.shells + 2 * pairP + 1);
+        const int sc = gload(args.pairs.shells + 2 * pairQ), sd = gload(args.pairs.shells + 2 * pairQ + 1);
         const int oa = gload(args.basis.bf_off + sa), ob = gload(args.basis.bf_off + sb);
         const int oc = gload(args.basis.bf_off + sc), od = gload(args.basis.bf_off + sd);
         const long long n = args.basis.nbf;
@@ -372,30 +429,36 @@ __global__ void __launch_bounds__(128) eri_class_kernel(const EriArgs args) {
                             Kbc[b][c] = fma(v, Dad[a][d], Kbc[b][c]);
                         }
             double *J = args.Jacc, *K = args.Kacc;
+            auto to_d = [](R x) -> double {
+                if constexpr (std::is_same<R, double>::value)
+                    return x;
+                else
+                    return f2d_bits(x);
+            };
 #pragma unroll
             for (int a = 0; a < NA; ++a)
 #pragma unroll
-                for (int b = 0; b < NB; ++b) atomicAdd(J + (oa + a) * n + ob + b, (double)(wJ * Jab[a][b]));
+                for (int b = 0; b < NB; ++b) atomicAdd(J + (oa + a) * n + ob + b, to_d(wJ * Jab[a][b]));
 #pragma unroll
             for (int c = 0; c < NC; ++c)
 #pragma unroll
-                for (int d = 0; d < ND; ++d) atomicAdd(J + (oc + c) * n + od + d, (double)(wJ * Jcd[c][d]));
+                for (int d = 0; d < ND; ++d) atomicAdd(J + (oc + c) * n + od + d, to_d(wJ * Jcd[c][d]));
 #pragma unroll
             for (int a = 0; a < NA; ++a)
 #pragma unroll
-                for (int c = 0; c < NC; ++c) atomicAdd(K + (oa + a) * n + oc + c, (double)(wK * Kac[a][c]));
+                for (int c = 0; c < NC; ++c) atomicAdd(K + (oa + a) * n + oc + c, to_d(wK * Kac[a][c]));
 #pragma unroll
             for (int b = 0; b < NB; ++b)
 #pragma unroll
-                for (int d = 0; d < ND; ++d) atomicAdd(K + (ob + b) * n + od + d, (double)(wK * Kbd[b][d]));
+                for (int d = 0; d < ND; ++d) atomicAdd(K + (ob + b) * n + od + d, to_d(wK * Kbd[b][d]));
 #pragma unroll
             for (int a = 0; a < NA; ++a)
 #pragma unroll
-                for (int d = 0; d < ND; ++d) atomicAdd(K + (oa + a) * n + od + d, (double)(wK * Kad[a][d]));
+                for (int d = 0; d < ND; ++d) atomicAdd(K + (oa + a) * n + od + d, to_d(wK * Kad[a][d]));
 #pragma unroll
             for (int b = 0; b < NB; ++b)
 #pragma unroll
-                for (int c = 0; c < NC; ++c) atomicAdd(K + (ob + b) * n + oc + c, (double)(wK * Kbc[b][c]));
+                for (int c = 0; c < NC; ++c) atomicAdd(K + (ob + b) * n + oc + c, to_d(wK * Kbc[b][c]));
         }
     }
 }
@@ -408,7 +471,9 @@ cudaError_t launch_eri_class(const EriArgs &args, int mode, int precision, cudaS
     if (args.nq <= 0) return cudaSuccess;
     const int threads = 128;
     long long blocks = (args.nq + threads - 1) / threads;
-    const long long cap = 152LL * 16 * 8;
+    // FP64: many blocks (FP64-bound, heavy-first order balances); FP32: about
+    // two waves of persistent blocks so the shared Boys table is loaded rarely.
+    const long long cap = precision == SQ_FP64 ? 152LL * 16 * 8 : 152LL * 16;
     if (blocks > cap) blocks = cap;
     (void)mode;  // per-thread kernels serve J/K launches only
     if (precision == SQ_FP64)
@@ -417,6 +482,21 @@ cudaError_t launch_eri_class(const EriArgs &args, int mode, int precision, cudaS
         eri_class_kernel<LA, LB, LC, LD, float, BOYS_FP64, MODE_JK><<<(int)blocks, threads, 0, stream>>>(args);
     else
         eri_class_kernel<LA, LB, LC, LD, float, BOYS_FP32, MODE_JK><<<(int)blocks, threads, 0, stream>>>(args);
+    return cudaGetLastError();
+}
+
+// FP32-only launcher (SQ_FP32) for the heavy classes whose full set of
+// variants would take too long to compile.
+template <int LA, int LB, int LC, int LD>
+cudaError_t launch_eri_class_f32(const EriArgs &args, int mode, int precision, cudaStream_t stream) {
+    (void)mode;
+    (void)precision;
+    if (args.nq <= 0) return cudaSuccess;
+    const int threads = 128;
+    long long blocks = (args.nq + threads - 1) / threads;
+    const long long cap = 152LL * 16;
+    if (blocks > cap) blocks = cap;
+    eri_class_kernel<LA, LB, LC, LD, float, BOYS_FP64, MODE_JK><<<(int)blocks, threads, 0, stream>>>(args);
     return cudaGetLastError();
 }
 

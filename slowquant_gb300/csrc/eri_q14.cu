@@ -1,0 +1,12 @@
+// eri_q14.cu -- per-thread J/K kernel of quartet class (dp|dp), FP32 integral
+// arithmetic with the FP64 Boys recursion only (its FP64 and all-FP32-Boys launches
+// run on the generic warp kernel).  The dispatch table in capi.cu calls this launcher.
+#include "eri.cuh"
+
+namespace sq {
+
+cudaError_t launch_qc_14_f32(const EriArgs &a, int mode, int prec, cudaStream_t s) {
+    return launch_eri_class_f32<2, 1, 2, 1>(a, mode, prec, s);
+}
+
+}  // namespace sq

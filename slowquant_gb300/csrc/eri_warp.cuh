@@ -134,7 +134,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
 
     for (long long qi = (long long)blockIdx.x * kWarpsPerBlock + warp; qi < args.nq; qi += nwarps) {
         const int2 pq = args.quartets[qi];
-        const int P = pq.x, Q = pq.y;
+        const int P = args.use_slots ? gload(args.slots.pair + pq.x) : pq.x;
+        const int Q = args.use_slots ? gload(args.slots.pair + pq.y) : pq.y;
         const int i0 = gload(pr.pp_off + P), i1 = gload(pr.pp_off + P + 1);
         const int k0 = gload(pr.pp_off + Q), k1 = gload(pr.pp_off + Q + 1);
         const R *hb = herm + gload(pr.herm_off + P);

@@ -35,6 +35,25 @@ __global__ void boys_table_kernel(double *tab64, float *tab32) {
     if (tab32) tab32[idx] = (float)val;
 }
 
+// Scaled Taylor blocks from the finished F grid: F_{m+j}(T_k)/j! (m < 15) and
+// exp(-T_k)/j! (block 15).
+__global__ void boys_taylor_kernel(double *tab64, float *tab32) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 16 * SQ_BOYS_NGRID * 8) return;
+    const int j = idx & 7, mk = idx >> 3;
+    const int m = mk / SQ_BOYS_NGRID, k = mk % SQ_BOYS_NGRID;
+    double fact = 1.0;
+    for (int t = 2; t <= j; ++t) fact *= t;
+    double val = 0.0;
+    if (j < kBoysTaylor64) {
+        const int col = (m == 15) ? SQ_BOYS_NCOL - 1 : m + j;
+        if (col < SQ_BOYS_NCOL) val = tab64[k * SQ_BOYS_NCOL + col] / fact;
+        if (m != 15 && col >= SQ_BOYS_NCOL - 1) val = 0.0;
+    }
+    tab64[SQ_BOYS_TAY64_OFF + idx] = val;
+    if (tab32 && j < 4) tab32[SQ_BOYS_TAY32_OFF + mk * 4 + j] = (float)val;
+}
+
 __global__ void boys_eval_kernel(int n_max, const double *z, long long nz, const double *tab, int mode,
                                  double *out) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -314,7 +333,38 @@ __global__ void quartets_expand_kernel(long long ntask, const int *bra, const in
         else hi = mid - 1;
     }
     const long long k = qi - offset[lo];
-    out[qi] = make_int2(bra[lo], ket_list[ket_start[lo] + k]);
+    out[qi] = make_int2(bra[lo], ket_list ? ket_list[ket_start[lo] + k] : (int)(ket_start[lo] + k));
+}
+
+// Slot layout: one thread per slot copies its primitive pairs' fields and
+// Hermite values from the pair (AoS) arrays.
+__global__ void slots_fill_kernel(const sq_basis basis, const sq_pairs pairs, sq_slots slots) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= slots.nslot) return;
+    const int P = slots.pair[s];
+    const int a = pairs.shells[2 * P], b = pairs.shells[2 * P + 1];
+    const int la = basis.l[a], lb = basis.l[b];
+    int E = 0;
+    for (int x = 0; x < ncart(la); ++x)
+        for (int y = 0; y < ncart(lb); ++y) E += herm_terms(la, x, lb, y);
+    const int n = slots.npp[s], stride = slots.pstride[s];
+    const long long pb = slots.pbase[s], hb = slots.hbase[s], NPP = slots.npp_total;
+    const long long src = pairs.pp_off[P];
+    const long long hsrc = pairs.herm_off[P];
+    for (int k = 0; k < n; ++k) {
+        const long long dst = pb + (long long)k * stride;
+        for (int f = 0; f < 5; ++f) {
+            const double v = pairs.prim[8 * (src + k) + f];
+            slots.prim[f * NPP + dst] = v;
+            if (slots.prim32) slots.prim32[f * NPP + dst] = (float)v;
+        }
+        for (int e = 0; e < E; ++e) {
+            const double v = pairs.herm[hsrc + (long long)k * E + e];
+            const long long d = hb + ((long long)k * E + e) * stride;
+            slots.herm[d] = v;
+            if (slots.herm32) slots.herm32[d] = (float)v;
+        }
+    }
 }
 
 __global__ void fock_build_kernel(int nbf, const double *H, const double *Jacc, const double *Kacc, double *F,
@@ -343,6 +393,8 @@ extern "C" int sq_boys_table(double *table64, float *table32, void *stream) {
     if (!table64) return set_error(SQ_ERR_ARG, "sq_boys_table: table64 is NULL");
     const int n = SQ_BOYS_NGRID * SQ_BOYS_NCOL;
     boys_table_kernel<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(table64, table32);
+    const int nt = 16 * SQ_BOYS_NGRID * 8;
+    boys_taylor_kernel<<<(nt + 127) / 128, 128, 0, (cudaStream_t)stream>>>(table64, table32);
     return check_launch("sq_boys_table");
 }
 
@@ -379,11 +431,20 @@ extern "C" int sq_quartets_expand(long long ntask, const int *bra, const int *ke
                                   void *stream) {
     if (ntask < 0 || nout < 0) return set_error(SQ_ERR_ARG, "sq_quartets_expand: negative size");
     if (ntask == 0 || nout == 0) return SQ_OK;
-    if (!bra || !ket_start || !count || !offset || !ket_list || !out_pairs)
+    if (!bra || !ket_start || !count || !offset || !out_pairs)
         return set_error(SQ_ERR_ARG, "sq_quartets_expand: NULL pointer");
     quartets_expand_kernel<<<(unsigned)((nout + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
         ntask, bra, ket_start, count, offset, ket_list, (int2 *)out_pairs, nout);
     return check_launch("sq_quartets_expand");
+}
+
+extern "C" int sq_slots_fill(const sq_basis *basis, const sq_pairs *pairs, sq_slots *slots, void *stream) {
+    if (!basis || !pairs || !slots || !slots->pair || !slots->npp || !slots->pbase || !slots->pstride ||
+        !slots->hbase || !slots->prim || !slots->herm)
+        return set_error(SQ_ERR_ARG, "sq_slots_fill: bad argument");
+    if (slots->nslot <= 0) return SQ_OK;
+    slots_fill_kernel<<<(slots->nslot + 127) / 128, 128, 0, (cudaStream_t)stream>>>(*basis, *pairs, *slots);
+    return check_launch("sq_slots_fill");
 }
 
 extern "C" int sq_fock_build(int nbf, const double *H, const double *Jacc, const double *Kacc, double *F, double *J,

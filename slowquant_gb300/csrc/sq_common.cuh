@@ -73,4 +73,31 @@ __host__ __device__ constexpr double dfact_odd(int n) {  // (2n-1)!!
     return r;
 }
 
+// f32 <-> f64 conversion with integer instructions.  On GB300 the hardware
+// conversion runs at the FP64 rate (about 1/58 of FP32), so FP32 kernels that
+// hand values to FP64 code convert on the integer pipe instead.  Valid for
+// zero and normal numbers (float denormals flush to zero; no inf/NaN inputs).
+__device__ __forceinline__ double f2d_bits(float x) {
+    const unsigned u = __float_as_uint(x);
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    const unsigned ex = (u >> 23) & 0xffu;
+    const unsigned long long body = ((unsigned long long)(ex + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)(ex == 0 ? sign : (sign | body)));
+}
+
+// Round-to-nearest-even f64 -> f32 (zero and the float normal range; smaller
+// magnitudes flush to zero, larger ones and NaN become +-inf).
+__device__ __forceinline__ float d2f_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const int ex = (int)((b >> 52) & 0x7ffu) - 896;
+    unsigned long long mant = b & 0xfffffffffffffULL;
+    mant += 0xfffffffULL + ((mant >> 29) & 1ULL);
+    const unsigned e2 = (unsigned)(ex + (int)(mant >> 52));
+    const unsigned m23 = (unsigned)((mant >> 29) & 0x7fffffu);
+    if (ex <= 0) return __uint_as_float(sign);
+    if (e2 >= 255u) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | (e2 << 23) | m23);
+}
+
 }  // namespace sq

@@ -27,7 +27,7 @@ import numpy as np
 import torch
 
 from . import _lib, screening
-from ._lib import SqBasis, SqPairs, SqQuartets, check, ptr
+from ._lib import SqBasis, SqPairs, SqQuartets, SqSlots, check, ptr
 from .molecule import _Molecule
 
 NCART = [1, 3, 6, 10]
@@ -120,8 +120,8 @@ class IntegralEngine:
         self.cbasis = b
 
         # Boys grid tables
-        self.tab64 = torch.empty(_lib.SQ_BOYS_NGRID * _lib.SQ_BOYS_NCOL, **f64)
-        self.tab32 = torch.empty(_lib.SQ_BOYS_NGRID * _lib.SQ_BOYS_NCOL, dtype=torch.float32, device=dev)
+        self.tab64 = torch.empty(_lib.SQ_BOYS_TAB64_SIZE, **f64)
+        self.tab32 = torch.empty(_lib.SQ_BOYS_TAB32_SIZE, dtype=torch.float32, device=dev)
         check(self.lib.sq_boys_table(ptr(self.tab64), ptr(self.tab32), self._stream()), "sq_boys_table")
 
         self.fp32 = fp32
@@ -129,6 +129,7 @@ class IntegralEngine:
         self._q = None
         self._quartet_cache: dict = {}
         self._jk_scratch = None
+        self._slots = None
 
     # ------------------------------------------------------------------ utils
     def _stream(self) -> int:
@@ -226,6 +227,68 @@ class IntegralEngine:
         cs[b, a] = q
         return cs
 
+    # ----------------------------------------------------------------- slots
+    @property
+    def slots(self) -> SqSlots:
+        """Slot layout (pairs in Schwarz-sorted group order, field-major data)."""
+        if self._slots is None:
+            self._build_slots()
+        return self._slots
+
+    def _build_slots(self) -> None:
+        q = self.pair_q
+        groups = screening.pair_groups(self.pair_class, self.pair_npa, self.pair_npb, q)
+        slot_pair = np.concatenate([g[1] for g in groups]).astype(np.int32) if groups else np.zeros(0, np.int32)
+        nslot = len(slot_pair)
+        npp = np.zeros(nslot, np.int32)
+        pbase = np.zeros(nslot, np.int32)
+        pstride = np.zeros(nslot, np.int32)
+        hbase = np.zeros(nslot, np.int64)
+        pos = 0
+        poff = 0
+        hoff = 0
+        for cls, members in groups:
+            n = len(members)
+            nppg = int(self.pair_np[members[0]])
+            la, lb = int(self.l[self.pair_shells[members[0], 0]]), int(self.l[self.pair_shells[members[0], 1]])
+            E = herm_size(la, lb)
+            sl = slice(pos, pos + n)
+            npp[sl] = nppg
+            pbase[sl] = poff + np.arange(n)
+            pstride[sl] = n
+            hbase[sl] = hoff + np.arange(n)
+            pos += n
+            poff += n * nppg
+            hoff += n * nppg * E
+        if poff >= 2**31:
+            raise RuntimeError("too many primitive pairs for int32 slot indexing")
+        self.slot_pair = slot_pair
+        self.slot_of_pair = np.empty(nslot, np.int32)
+        self.slot_of_pair[slot_pair] = np.arange(nslot, dtype=np.int32)
+        dev = self.device
+        i32 = dict(dtype=torch.int32, device=dev)
+        self.t_slot_pair = torch.tensor(slot_pair, **i32)
+        self.t_slot_of_pair = torch.tensor(self.slot_of_pair, **i32)
+        self.t_slot_npp = torch.tensor(npp, **i32)
+        self.t_slot_pbase = torch.tensor(pbase, **i32)
+        self.t_slot_pstride = torch.tensor(pstride, **i32)
+        self.t_slot_hbase = torch.tensor(hbase, dtype=torch.int64, device=dev)
+        self.t_slot_prim = torch.empty(max(5 * poff, 1), dtype=torch.float64, device=dev)
+        self.t_slot_herm = torch.empty(max(hoff, 1), dtype=torch.float64, device=dev)
+        self.t_slot_prim32 = torch.empty(max(5 * poff, 1), dtype=torch.float32, device=dev) if self.fp32 else None
+        self.t_slot_herm32 = torch.empty(max(hoff, 1), dtype=torch.float32, device=dev) if self.fp32 else None
+        s = SqSlots()
+        s.nslot, s.npp_total, s.nherm_total = nslot, poff, hoff
+        s.pair, s.npp, s.pbase, s.pstride, s.hbase = (ptr(self.t_slot_pair), ptr(self.t_slot_npp),
+                                                      ptr(self.t_slot_pbase), ptr(self.t_slot_pstride),
+                                                      ptr(self.t_slot_hbase))
+        s.prim, s.herm = ptr(self.t_slot_prim), ptr(self.t_slot_herm)
+        s.prim32, s.herm32 = ptr(self.t_slot_prim32), ptr(self.t_slot_herm32)
+        self._slots = s
+        if nslot:
+            check(self.lib.sq_slots_fill(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(s),
+                                         self._stream()), "sq_slots_fill")
+
     # -------------------------------------------------------------- quartets
     def quartets(self, threshold: float, fp32_threshold: float | None = None, q: np.ndarray | None = None):
         """Unique screened quartets.  Returns one QuartetList, or (fp64, fp32) lists
@@ -239,6 +302,7 @@ class IntegralEngine:
         qv = self.pair_q if own else np.asarray(q, dtype=np.float64)
         lists, ket_list = screening.build_tasks(self.pair_class, self.pair_npa, self.pair_npb, qv, threshold,
                                                 fp32_threshold)
+        self.slots  # canonical slot numbering (from the engine's own Schwarz factors)
         out = [self._expand(t, ket_list) for t in lists]
         res = out[0] if len(out) == 1 else (out[0], out[1])
         if own:
@@ -251,11 +315,12 @@ class IntegralEngine:
         dev = self.device
         pairs = torch.empty((max(nq, 1), 2), dtype=torch.int32, device=dev)
         if nq:
-            t_bra = torch.tensor(bra, dtype=torch.int32, device=dev)
+            # quartet entries are slot ids: map bra pair ids and the ket order
+            t_bra = torch.tensor(self.slot_of_pair[bra], dtype=torch.int32, device=dev)
             t_kst = torch.tensor(kst, dtype=torch.int32, device=dev)
             t_cnt = torch.tensor(cnt.astype(np.int32), dtype=torch.int32, device=dev)
             t_off = torch.tensor(toff, dtype=torch.int64, device=dev)
-            t_ket = torch.tensor(ket_list, dtype=torch.int32, device=dev)
+            t_ket = torch.tensor(self.slot_of_pair[ket_list], dtype=torch.int32, device=dev)
             check(self.lib.sq_quartets_expand(len(bra), ptr(t_bra), ptr(t_kst), ptr(t_cnt), ptr(t_off),
                                               ptr(t_ket), ptr(pairs), nq, self._stream()), "sq_quartets_expand")
         return QuartetList(pairs, off)
@@ -286,8 +351,8 @@ class IntegralEngine:
         else:
             ql = self.quartets(threshold, q=q)
         qs = ql.cstruct()
-        check(self.lib.sq_eri_dense(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(qs),
-                                    ptr(self.tab64), ptr(V), self._stream()), "sq_eri_dense")
+        check(self.lib.sq_eri_dense(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(self.slots),
+                                    ctypes.byref(qs), ptr(self.tab64), ptr(V), self._stream()), "sq_eri_dense")
         return V
 
     def _scratch(self):
@@ -313,9 +378,9 @@ class IntegralEngine:
             if ql.nquartet == 0:
                 continue
             qs = ql.cstruct()
-            check(self.lib.sq_jk(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(qs),
-                                 ptr(self.tab64), ptr(self.tab32), ptr(D), ptr(D32), ptr(Jacc), ptr(Kacc),
-                                 _lib.PRECISIONS[prec], self._stream()), "sq_jk")
+            check(self.lib.sq_jk(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(self.slots),
+                                 ctypes.byref(qs), ptr(self.tab64), ptr(self.tab32), ptr(D), ptr(D32), ptr(Jacc),
+                                 ptr(Kacc), _lib.PRECISIONS[prec], self._stream()), "sq_jk")
         return Jacc, Kacc
 
     def jk(self, D: torch.Tensor, threshold: float = 1e-12, precision: str = "fp64",

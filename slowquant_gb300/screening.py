@@ -14,7 +14,10 @@ cs[i,j] * cs[k,l] < threshold.  Here the unique quartets are enumerated as
 * for a bra pair with factor x the surviving kets of a group are the prefix
   with x * q_ket >= threshold (the same product test as the reference), and
   with a second threshold that prefix splits into a large-bound (FP64) part
-  and a small-bound (FP32) part.
+  and a small-bound (FP32) part;
+* inside a quartet class, group pairs are emitted heaviest first (primitive
+  quartets per contracted quartet), so the device's block scheduler balances
+  the load across SMs.
 
 ``build_tasks`` returns per quartet class the (bra pair, ket start, count)
 tasks; the device kernel sq_quartets_expand turns them into the flat list.
@@ -75,6 +78,8 @@ def build_tasks(pair_class, npa, npb, q, threshold: float, fp32_threshold: float
     gstart = np.concatenate([[0], np.cumsum([len(g[1]) for g in groups])]).astype(np.int64)
     nlists = 1 if fp32_threshold is None else 2
     lists = [{c: [] for c in range(NQCLASS)} for _ in range(nlists)]
+    npp = np.asarray(npa, dtype=np.int64) * np.asarray(npb, dtype=np.int64)
+    pending = [{c: [] for c in range(NQCLASS)} for _ in range(nlists)]
     for g1, (c1, m1) in enumerate(groups):
         x = q[m1]
         for g2 in range(g1 + 1):
@@ -91,11 +96,20 @@ def build_tasks(pair_class, npa, npb, q, threshold: float, fp32_threshold: float
                 c64 = np.minimum(prefix_counts(x, qk, fp32_threshold), cnt)
                 bounds = [(np.zeros_like(cnt), c64), (c64, cnt)]
             qc = quartet_class(c1, c2)
+            # primitive quartets per contracted quartet of this group pair
+            cost = int(npp[m1[0]] * npp[m2[0]])
             for li, (lo, hi) in enumerate(bounds):
                 n = hi - lo
                 keep = n > 0
                 if keep.any():
-                    lists[li][qc].append((m1[keep], gstart[g2] + lo[keep], n[keep]))
+                    pending[li][qc].append((cost, g1, g2, (m1[keep], gstart[g2] + lo[keep], n[keep])))
+    # Heaviest group pairs first inside each class: every quartet of a group pair
+    # costs the same, so this is longest-processing-time-first order for the
+    # hardware block scheduler (light blocks fill the tail).
+    for li in range(nlists):
+        for qc in range(NQCLASS):
+            for _, _, _, task in sorted(pending[li][qc], key=lambda t: (-t[0], t[1], t[2])):
+                lists[li][qc].append(task)
     return lists, ket_list
 
 
