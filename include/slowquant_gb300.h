@@ -184,6 +184,23 @@ int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, c
           const double *table64, const float *table32, const double *D, float *D32, double *Jacc, double *Kacc,
           int precision, void *stream);
 
+/* J/K build for callers that cannot allocate device memory.  No counterpart
+ * in the reference (it has no device code).  Same arguments and results as
+ * sq_jk, minus D32: the FP32 density scratch that FP32 launches need lives in
+ * a fixed array inside this library (SQ_NOALLOC_MAX_NBF^2 floats, 4 MiB, held
+ * on every GPU that loads the library until the process exits).  It serves
+ * hosts that own all device memory, streams whose capture mode forbids
+ * allocation, and loops that cannot afford cudaMalloc's synchronisation.
+ * nbf > SQ_NOALLOC_MAX_NBF is rejected with SQ_ERR_ARG.  The first call on a
+ * device looks up the array's device address; make it before any stream
+ * capture.  Calls share the array, so calls that overlap on the GPU race and
+ * must be serialised by the caller; each FP32 call overwrites the array
+ * before reading it.  Allocates nothing. */
+#define SQ_NOALLOC_MAX_NBF 1024
+int sq_jk_noalloc(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, const sq_quartets *quartets,
+                  const double *table64, const float *table32, const double *D, double *Jacc, double *Kacc,
+                  int precision, void *stream);
+
 /* F = H + J - K/2 with J = (Jacc + Jacc^T)/2, K = (Kacc + Kacc^T)/2
  * (hartreefock_in_memory.py:57); J and K may be NULL. */
 int sq_fock_build(int nbf, const double *H, const double *Jacc, const double *Kacc, double *F, double *J,

@@ -26,6 +26,7 @@ SQ_FP64 = 0
 SQ_FP32 = 1
 SQ_FP32_BOYS32 = 2
 SQ_OPT_GENERIC_MIN_L = 1
+SQ_NOALLOC_MAX_NBF = 1024
 
 PRECISIONS = {"fp64": SQ_FP64, "fp32": SQ_FP32, "fp32_boys32": SQ_FP32_BOYS32}
 
@@ -90,6 +91,8 @@ def lib() -> ctypes.CDLL:
         L.sq_jk.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
                             ctypes.POINTER(SqQuartets), _p, _p, _p, _p, _p, _p, ctypes.c_int, _p]
         L.sq_slots_fill.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots), _p]
+        L.sq_jk_noalloc.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
+                                    ctypes.POINTER(SqQuartets), _p, _p, _p, _p, _p, ctypes.c_int, _p]
         L.sq_fock_build.argtypes = [ctypes.c_int, _p, _p, _p, _p, _p, _p, _p]
         L.sq_one_electron.argtypes = [ctypes.POINTER(SqBasis), _p, _p, _p, _p, _p]
         L.sq_quartets_expand.argtypes = [ctypes.c_longlong, _p, _p, _p, _p, _p, _p, ctypes.c_longlong, _p]
@@ -101,7 +104,7 @@ def lib() -> ctypes.CDLL:
 EXPORTED = [
     "sq_version", "sq_last_error", "sq_set_option", "sq_get_option", "sq_boys_table", "sq_boys",
     "sq_pair_prep", "sq_schwarz", "sq_eri_dense", "sq_jk", "sq_fock_build", "sq_one_electron",
-    "sq_quartets_expand", "sq_fma_probe", "sq_slots_fill",
+    "sq_quartets_expand", "sq_fma_probe", "sq_slots_fill", "sq_jk_noalloc",
 ]
 
 
