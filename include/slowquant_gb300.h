@@ -69,6 +69,18 @@ typedef struct sq_basis {
                                   1/sqrt((2x-1)!!(2y-1)!!(2z-1)!!) is applied by the kernels */
     const double *atom_xyz;    /* [natom][3], bohr */
     const double *atom_charge; /* [natom] */
+    const int *shell_atom;     /* [nshell] atom that carries each shell (used by the gradient kernels) */
+    /* Batches of independent molecules (all NULL / 0 for one molecule): the
+     * n x n matrices (D, J, K, S, T, V) of molecule i are packed blocks;
+     * element (mu, nu) of the molecule that owns shells s, t lives at
+     * mat_base[s] + (bf_off[s] + a) * mat_ld[s] + bf_off[t] + b, with bf_off
+     * molecule-local; mat_total is the packed length.  The one-electron kernel
+     * sums the nuclear attraction over atoms atom_begin[s] <= A < atom_end[s]. */
+    const long long *mat_base; /* [nshell] */
+    const int *mat_ld;         /* [nshell] */
+    long long mat_total;
+    const int *atom_begin;     /* [nshell] */
+    const int *atom_end;       /* [nshell] */
 } sq_basis;
 
 /* Shell pairs and their primitive-pair (Hermite) data.  The caller fills the
@@ -132,6 +144,14 @@ const char *sq_last_error(void);
 #define SQ_OPT_GENERIC_MIN_L 1
 int sq_set_option(int key, long long value);
 long long sq_get_option(int key);
+
+/* Launch shape ("tile") of the J/K kernels of one quartet class and precision
+ * (no reference counterpart), set by the autotuner (slowquant_gb300.autotune):
+ * threads per block (32..128 for the per-quartet kernels; the generic warp
+ * kernel always runs 4 warps) and the grid cap in blocks (quartets beyond
+ * blocks x threads are taken by a grid-stride loop).  threads = 0 restores
+ * the built-in default. */
+int sq_set_launch_config(int qclass, int precision, int threads, long long max_blocks);
 
 /* Fill the FP64 Boys table (SQ_BOYS_TAB64_SIZE doubles) and, if
  * table32 != NULL, the FP32 table (SQ_BOYS_TAB32_SIZE floats).  Replaces nothing: the reference
@@ -220,6 +240,22 @@ int sq_one_electron(const sq_basis *basis, const double *table64, double *S, dou
 int sq_quartets_expand(long long ntask, const int *bra, const int *ket_start, const int *count,
                        const long long *offset, const int *ket_list, int *out_pairs, long long nquartet,
                        void *stream);
+
+/* RHF nuclear gradient, two-electron part (no reference counterpart: the
+ * reference has no gradients).  For every unique quartet of `quartets` (slot
+ * ids) the derivative integrals are formed on the fly and contracted with the
+ * two-particle density of D, never stored:
+ *   grad[atom][xyz] += (m/2) sum_abcd Gamma'_abcd d(ab|cd)/dR,
+ *   Gamma'_abcd = D_ab D_cd - (D_ac D_bd + D_ad D_bc)/4,  m = permutational weight.
+ * grad is [natom][3] FP64, accumulated (caller zeroes).  FP64 arithmetic. */
+int sq_grad_2e(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, const sq_quartets *quartets,
+               const double *table64, const double *D, double *grad, void *stream);
+
+/* RHF nuclear gradient, one-electron part: grad += sum_ab D_ab dH_ab/dR -
+ * sum_ab W_ab dS_ab/dR (kinetic energy, nuclear attraction including the
+ * derivative with respect to each nucleus, overlap), for D, W [nbf][nbf]. */
+int sq_grad_1e(const sq_basis *basis, const double *table64, const double *D, const double *W, double *grad,
+               void *stream);
 
 /* Arithmetic-pipe probe (no reference counterpart): blocks x 256 threads each
  * run `iters` iterations of 8 independent FMA chains in FP64 (precision

@@ -37,7 +37,8 @@ class SqBasis(ctypes.Structure):
     _fields_ = [
         ("nshell", ctypes.c_int), ("nbf", ctypes.c_int), ("natom", ctypes.c_int), ("nprim_total", ctypes.c_int),
         ("center", _p), ("l", _p), ("nprim", _p), ("prim_off", _p), ("bf_off", _p), ("exps", _p),
-        ("coefs", _p), ("atom_xyz", _p), ("atom_charge", _p),
+        ("coefs", _p), ("atom_xyz", _p), ("atom_charge", _p), ("shell_atom", _p),
+        ("mat_base", _p), ("mat_ld", _p), ("mat_total", ctypes.c_longlong), ("atom_begin", _p), ("atom_end", _p),
     ]
 
 
@@ -81,6 +82,7 @@ def lib() -> ctypes.CDLL:
         L.sq_get_option.restype = ctypes.c_longlong
         L.sq_get_option.argtypes = [ctypes.c_int]
         L.sq_set_option.argtypes = [ctypes.c_int, ctypes.c_longlong]
+        L.sq_set_launch_config.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_longlong]
         L.sq_boys_table.argtypes = [_p, _p, _p]
         L.sq_boys.argtypes = [ctypes.c_int, _p, ctypes.c_longlong, _p, ctypes.c_int, _p, _p]
         L.sq_pair_prep.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), _p]
@@ -91,6 +93,9 @@ def lib() -> ctypes.CDLL:
         L.sq_jk.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
                             ctypes.POINTER(SqQuartets), _p, _p, _p, _p, _p, _p, ctypes.c_int, _p]
         L.sq_slots_fill.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots), _p]
+        L.sq_grad_2e.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
+                                 ctypes.POINTER(SqQuartets), _p, _p, _p, _p]
+        L.sq_grad_1e.argtypes = [ctypes.POINTER(SqBasis), _p, _p, _p, _p, _p]
         L.sq_jk_noalloc.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
                                     ctypes.POINTER(SqQuartets), _p, _p, _p, _p, _p, ctypes.c_int, _p]
         L.sq_fock_build.argtypes = [ctypes.c_int, _p, _p, _p, _p, _p, _p, _p]
@@ -102,9 +107,9 @@ def lib() -> ctypes.CDLL:
 
 
 EXPORTED = [
-    "sq_version", "sq_last_error", "sq_set_option", "sq_get_option", "sq_boys_table", "sq_boys",
+    "sq_version", "sq_last_error", "sq_set_option", "sq_get_option", "sq_set_launch_config", "sq_boys_table", "sq_boys",
     "sq_pair_prep", "sq_schwarz", "sq_eri_dense", "sq_jk", "sq_fock_build", "sq_one_electron",
-    "sq_quartets_expand", "sq_fma_probe", "sq_slots_fill", "sq_jk_noalloc",
+    "sq_quartets_expand", "sq_fma_probe", "sq_slots_fill", "sq_jk_noalloc", "sq_grad_2e", "sq_grad_1e",
 ]
 
 

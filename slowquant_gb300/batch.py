@@ -1,0 +1,460 @@
+"""Many independent molecules in one set of kernel launches.
+
+A batch is one block-diagonal system: shells of all molecules are
+concatenated, shell pairs and shell quartets exist only inside a molecule, and
+the n_i x n_i matrices (D, J, K, S, T, V, F) of molecule i are packed blocks
+of one flat device buffer.  Molecules are ordered by basis size, so the
+blocks of equal-size molecules form a [count, n, n] tensor view: the SCF's
+linear algebra (DIIS, eigh) runs batched per size group, and every Fock
+build of the whole batch is one launch per quartet class over all molecules'
+quartets (heavy-first order across molecules).  Setup (pairs, Schwarz,
+one-electron integrals) is also one launch each for the batch.
+
+The steady-state Fock build (zeroing, the class launches, F assembly) is
+captured once in a CUDA graph and replayed every SCF iteration.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib, screening
+from ._lib import SqBasis, SqPairs, SqQuartets, SqSlots, check, ptr
+from .engine import QuartetList, herm_size
+from .molecule import _Molecule
+
+
+@dataclass
+class SizeGroup:
+    nbf: int
+    mols: list[int]  # molecule indices (batch order)
+    offset: int  # element offset of the group's first block in the packed buffers
+    nocc: int
+
+
+class BatchEngine:
+    """Integral engine for a batch of independent molecules on one GPU."""
+
+    def __init__(self, molecules: list[_Molecule], device=None, fp32: bool = True):
+        if not torch.cuda.is_available():
+            raise RuntimeError("slowquant_gb300 needs a CUDA device; there is no CPU fallback")
+        self.lib = _lib.lib()
+        self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        order = sorted(range(len(molecules)), key=lambda i: (molecules[i].number_bf, i))
+        self.order = order
+        self.mols = [molecules[i] for i in order]
+        self.nmol = len(self.mols)
+        self.fp32 = fp32
+        dev = self.device
+        # ---- concatenated basis with packed matrix addressing
+        l, nprim, bf_off, centers, exps, coefs = [], [], [], [], [], []
+        mat_base, mat_ld, atom_begin, atom_end, shell_atom, shell_mol = [], [], [], [], [], []
+        atom_xyz, atom_charge = [], []
+        base = 0
+        natom = 0
+        self.mol_base, self.mol_nbf, self.mol_shell0 = [], [], []
+        for mi, m in enumerate(self.mols):
+            n = m.number_bf
+            self.mol_base.append(base)
+            self.mol_nbf.append(n)
+            self.mol_shell0.append(len(l))
+            coords = m.atom_coordinates
+            origin = coords.mean(axis=0)
+            for s in m.shells:
+                l.append(s.angular_momentum)
+                nprim.append(len(s.exponents))
+                bf_off.append(int(s.bf_idx[0]))
+                centers.append(np.asarray(s.center) - origin)
+                exps.append(s.exponents)
+                coefs.append(s.component_independent_coefficients())
+                mat_base.append(base)
+                mat_ld.append(n)
+                atom_begin.append(natom)
+                atom_end.append(natom + len(m.atoms))
+                shell_atom.append(natom + m.atoms.index(s.origin_atom))
+                shell_mol.append(mi)
+            atom_xyz.append(coords - origin)
+            atom_charge.append(m.atom_charges)
+            natom += len(m.atoms)
+            base += n * n
+        self.mat_total = base
+        self.l = np.array(l, dtype=np.int32)
+        if self.l.max() > _lib.SQ_MAX_L:
+            raise NotImplementedError("batched ERI kernels support shells up to d")
+        self.nprim = np.array(nprim, dtype=np.int32)
+        self.shell_mol = np.array(shell_mol, dtype=np.int32)
+        prim_off = np.concatenate([[0], np.cumsum(self.nprim)[:-1]]).astype(np.int32)
+        f64 = dict(dtype=torch.float64, device=dev)
+        i32 = dict(dtype=torch.int32, device=dev)
+        self._keep = [
+            torch.tensor(np.array(centers), **f64), torch.tensor(self.l, **i32), torch.tensor(self.nprim, **i32),
+            torch.tensor(prim_off, **i32), torch.tensor(np.array(bf_off, dtype=np.int32), **i32),
+            torch.tensor(np.concatenate(exps), **f64), torch.tensor(np.concatenate(coefs), **f64),
+            torch.tensor(np.concatenate(atom_xyz), **f64).reshape(-1, 3).contiguous(),
+            torch.tensor(np.concatenate(atom_charge), **f64), torch.tensor(np.array(shell_atom, np.int32), **i32),
+            torch.tensor(np.array(mat_base, np.int64), dtype=torch.int64, device=dev),
+            torch.tensor(np.array(mat_ld, np.int32), **i32), torch.tensor(np.array(atom_begin, np.int32), **i32),
+            torch.tensor(np.array(atom_end, np.int32), **i32),
+        ]
+        k = self._keep
+        b = SqBasis()
+        b.nshell, b.nbf, b.natom, b.nprim_total = len(l), max(self.mol_nbf), natom, int(self.nprim.sum())
+        b.center, b.l, b.nprim, b.prim_off, b.bf_off = ptr(k[0]), ptr(k[1]), ptr(k[2]), ptr(k[3]), ptr(k[4])
+        b.exps, b.coefs, b.atom_xyz, b.atom_charge, b.shell_atom = ptr(k[5]), ptr(k[6]), ptr(k[7]), ptr(k[8]), ptr(k[9])
+        b.mat_base, b.mat_ld, b.mat_total = ptr(k[10]), ptr(k[11]), self.mat_total
+        b.atom_begin, b.atom_end = ptr(k[12]), ptr(k[13])
+        self.cbasis = b
+        self.tab64 = torch.empty(_lib.SQ_BOYS_TAB64_SIZE, **f64)
+        self.tab32 = torch.empty(_lib.SQ_BOYS_TAB32_SIZE, dtype=torch.float32, device=dev)
+        check(self.lib.sq_boys_table(ptr(self.tab64), ptr(self.tab32), self._stream()), "sq_boys_table")
+        # size groups (contiguous in the packed buffers)
+        self.groups: list[SizeGroup] = []
+        for mi, m in enumerate(self.mols):
+            n = m.number_bf
+            if not self.groups or self.groups[-1].nbf != n:
+                self.groups.append(SizeGroup(n, [], self.mol_base[mi], m.number_electrons // 2))
+            self.groups[-1].mols.append(mi)
+        self._build_pairs()
+        self._schwarz()
+        self._build_slots()
+        self._lists: dict = {}
+        self._graphs: dict = {}
+
+    def _stream(self) -> int:
+        return _lib.stream_handle(self.device)
+
+    # ------------------------------------------------------------- pairs
+    def _build_pairs(self) -> None:
+        a_all, b_all = [], []
+        for mi, m in enumerate(self.mols):
+            s0 = self.mol_shell0[mi]
+            ns = m.number_shell
+            i, j = np.triu_indices(ns)
+            i += s0
+            j += s0
+            li, lj = self.l[i], self.l[j]
+            a_all.append(np.where(li >= lj, i, j))
+            b_all.append(np.where(li >= lj, j, i))
+        a = np.concatenate(a_all)
+        b = np.concatenate(b_all)
+        la, lb = self.l[a], self.l[b]
+        pc = la * (la + 1) // 2 + lb
+        order = np.argsort(pc, kind="stable")
+        a, b, pc = a[order], b[order], pc[order]
+        self.pair_shells = np.stack([a, b], 1).astype(np.int32)
+        self.pair_class = pc.astype(np.int32)
+        self.pair_mol = self.shell_mol[a]
+        self.pair_npa, self.pair_npb = self.nprim[a], self.nprim[b]
+        self.pair_np = (self.pair_npa * self.pair_npb).astype(np.int64)
+        self.npair = len(a)
+        hs = np.array([herm_size(int(x), int(y)) for x, y in zip(la[order], lb[order])], dtype=np.int64)
+        pp_off = np.concatenate([[0], np.cumsum(self.pair_np)]).astype(np.int64)
+        herm_off = np.concatenate([[0], np.cumsum(self.pair_np * hs)[:-1]]).astype(np.int64)
+        nprimpair, nherm = int(pp_off[-1]), int((self.pair_np * hs).sum())
+        dev = self.device
+        self.t_pair = [
+            torch.tensor(self.pair_shells, dtype=torch.int32, device=dev),
+            torch.tensor(pp_off.astype(np.int32), dtype=torch.int32, device=dev),
+            torch.tensor(herm_off, dtype=torch.int64, device=dev),
+            torch.empty(nprimpair * 8, dtype=torch.float64, device=dev),
+            torch.empty(max(nherm, 1), dtype=torch.float64, device=dev),
+            torch.empty(nprimpair * 8, dtype=torch.float32, device=dev) if self.fp32 else None,
+            torch.empty(max(nherm, 1), dtype=torch.float32, device=dev) if self.fp32 else None,
+        ]
+        t = self.t_pair
+        p = SqPairs()
+        p.npair, p.nprimpair = self.npair, nprimpair
+        p.shells, p.pp_off, p.herm_off, p.prim, p.herm = ptr(t[0]), ptr(t[1]), ptr(t[2]), ptr(t[3]), ptr(t[4])
+        p.prim32, p.herm32 = ptr(t[5]), ptr(t[6])
+        self.cpairs = p
+        check(self.lib.sq_pair_prep(ctypes.byref(self.cbasis), ctypes.byref(p), self._stream()), "sq_pair_prep")
+
+    def _schwarz(self) -> None:
+        lists = {}
+        for pc in np.unique(self.pair_class):
+            idx = np.nonzero(self.pair_class == pc)[0].astype(np.int32)
+            lists[screening.quartet_class(int(pc), int(pc))] = np.stack([idx, idx], 1)
+        off = np.zeros(_lib.SQ_MAX_QCLASS + 1, np.int64)
+        parts = []
+        for c in range(_lib.SQ_MAX_QCLASS):
+            arr = lists.get(c)
+            off[c + 1] = off[c] + (0 if arr is None else len(arr))
+            if arr is not None:
+                parts.append(arr)
+        ql = QuartetList(torch.tensor(np.concatenate(parts), dtype=torch.int32, device=self.device), off)
+        q = torch.zeros(self.npair, dtype=torch.float64, device=self.device)
+        qs = ql.cstruct()
+        check(self.lib.sq_schwarz(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(qs),
+                                  ptr(self.tab64), ptr(q), self._stream()), "sq_schwarz")
+        self.pair_q = q.cpu().numpy()
+
+    def _build_slots(self) -> None:
+        # groups keyed by (molecule, class, primitive counts), sorted by descending q
+        key_class = self.pair_mol.astype(np.int64) * 64 + self.pair_class
+        groups = screening.pair_groups(key_class, self.pair_npa, self.pair_npb, self.pair_q)
+        self.slot_groups = groups
+        slot_pair = np.concatenate([g[1] for g in groups]).astype(np.int32)
+        nslot = len(slot_pair)
+        npp, pbase, pstride = (np.zeros(nslot, np.int32) for _ in range(3))
+        hbase = np.zeros(nslot, np.int64)
+        pos = poff = hoff = 0
+        for _, members in groups:
+            n = len(members)
+            nppg = int(self.pair_np[members[0]])
+            la, lb = int(self.l[self.pair_shells[members[0], 0]]), int(self.l[self.pair_shells[members[0], 1]])
+            E = herm_size(la, lb)
+            sl = slice(pos, pos + n)
+            npp[sl] = nppg
+            pbase[sl] = poff + np.arange(n)
+            pstride[sl] = n
+            hbase[sl] = hoff + np.arange(n)
+            pos += n
+            poff += n * nppg
+            hoff += n * nppg * E
+        self.slot_pair = slot_pair
+        self.slot_of_pair = np.empty(nslot, np.int32)
+        self.slot_of_pair[slot_pair] = np.arange(nslot, dtype=np.int32)
+        dev = self.device
+        i32 = dict(dtype=torch.int32, device=dev)
+        self.t_slot = [
+            torch.tensor(slot_pair, **i32), torch.tensor(npp, **i32), torch.tensor(pbase, **i32),
+            torch.tensor(pstride, **i32), torch.tensor(hbase, dtype=torch.int64, device=dev),
+            torch.empty(5 * poff, dtype=torch.float64, device=dev), torch.empty(max(hoff, 1), dtype=torch.float64, device=dev),
+            torch.empty(5 * poff, dtype=torch.float32, device=dev) if self.fp32 else None,
+            torch.empty(max(hoff, 1), dtype=torch.float32, device=dev) if self.fp32 else None,
+        ]
+        t = self.t_slot
+        s = SqSlots()
+        s.nslot, s.npp_total, s.nherm_total = nslot, poff, hoff
+        s.pair, s.npp, s.pbase, s.pstride, s.hbase = ptr(t[0]), ptr(t[1]), ptr(t[2]), ptr(t[3]), ptr(t[4])
+        s.prim, s.herm, s.prim32, s.herm32 = ptr(t[5]), ptr(t[6]), ptr(t[7]), ptr(t[8])
+        self.slots = s
+        check(self.lib.sq_slots_fill(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(s),
+                                     self._stream()), "sq_slots_fill")
+
+    # ---------------------------------------------------------- quartets
+    def quartets(self, threshold: float, fp32_threshold: float | None = None):
+        """Screened unique quartets of every molecule (slot ids), one segment per class,
+        tasks of all molecules merged heaviest first."""
+        key = (threshold, fp32_threshold)
+        if key in self._lists:
+            return self._lists[key]
+        nl = 1 if fp32_threshold is None else 2
+        merged = [{c: [] for c in range(screening.NQCLASS)} for _ in range(nl)]
+        for mi in range(self.nmol):
+            sel = np.nonzero(self.pair_mol == mi)[0]
+            lists, ket = screening.build_tasks(self.pair_class[sel], self.pair_npa[sel], self.pair_npb[sel],
+                                               self.pair_q[sel], threshold, fp32_threshold)
+            # a molecule's groups are consecutive slots in the same order, so the
+            # kets of one task are consecutive slots starting at slot_of_pair[ket[start]]
+            ket_slots = self.slot_of_pair[sel[ket]]
+            for li in range(nl):
+                for c in range(screening.NQCLASS):
+                    for bra, kst, cnt in lists[li][c]:
+                        cost = int(self.pair_np[sel[bra[0]]] * self.pair_np[sel[ket[kst[0]]]])
+                        merged[li][c].append((cost, self.slot_of_pair[sel[bra]], ket_slots[kst], cnt))
+        out = []
+        for li in range(nl):
+            tasks = {c: [(b, k, n) for _, b, k, n in sorted(merged[li][c], key=lambda t: -t[0])]
+                     for c in range(screening.NQCLASS)}
+            bra, kst, cnt, toff, off = screening.flatten_tasks(tasks)
+            nq = int(off[-1])
+            pairs = torch.empty((max(nq, 1), 2), dtype=torch.int32, device=self.device)
+            if nq:
+                dev = self.device
+                tb = torch.tensor(bra, dtype=torch.int32, device=dev)
+                tk = torch.tensor(kst, dtype=torch.int32, device=dev)
+                tc = torch.tensor(cnt.astype(np.int32), dtype=torch.int32, device=dev)
+                to = torch.tensor(toff, dtype=torch.int64, device=dev)
+                check(self.lib.sq_quartets_expand(len(bra), ptr(tb), ptr(tk), ptr(tc), ptr(to), None, ptr(pairs),
+                                                  nq, self._stream()), "sq_quartets_expand")
+                torch.cuda.current_stream(self.device).synchronize()
+            out.append(QuartetList(pairs, off))
+        res = out[0] if nl == 1 else (out[0], out[1])
+        self._lists[key] = res
+        return res
+
+    # ---------------------------------------------------------- matrices
+    def one_electron(self):
+        S = torch.zeros(self.mat_total, dtype=torch.float64, device=self.device)
+        T = torch.zeros_like(S)
+        V = torch.zeros_like(S)
+        check(self.lib.sq_one_electron(ctypes.byref(self.cbasis), ptr(self.tab64), ptr(S), ptr(T), ptr(V),
+                                       self._stream()), "sq_one_electron")
+        return S, T, V
+
+    def view(self, flat: torch.Tensor, g: SizeGroup) -> torch.Tensor:
+        n = g.nbf
+        return flat[g.offset:g.offset + len(g.mols) * n * n].view(len(g.mols), n, n)
+
+    def jk_accumulate(self, D: torch.Tensor, Jacc: torch.Tensor, Kacc: torch.Tensor, D32: torch.Tensor,
+                      lists, precs) -> None:
+        Jacc.zero_()
+        Kacc.zero_()
+        for ql, prec in zip(lists, precs):
+            if ql.nquartet == 0:
+                continue
+            qs = ql.cstruct()
+            check(self.lib.sq_jk(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(self.slots),
+                                 ctypes.byref(qs), ptr(self.tab64), ptr(self.tab32), ptr(D), ptr(D32), ptr(Jacc),
+                                 ptr(Kacc), _lib.PRECISIONS[prec], self._stream()), "sq_jk")
+
+
+class _BatchDIIS:
+    """Pulay DIIS (diis.py:4-66 semantics) for a [count, n, n] group, ring buffer of 6."""
+
+    def __init__(self, count: int, n: int, device, nsave: int = 6):
+        self.F = torch.zeros((nsave, count, n, n), dtype=torch.float64, device=device)
+        self.E = torch.zeros_like(self.F)
+        self.nsave = nsave
+        self.k = 0  # vectors stored
+        self.head = 0
+        self.last_error = None
+
+    def extrapolate(self, F, D, S):
+        if F.shape[-1] == 2:
+            return F
+        err = F @ D @ S - S @ D @ F
+        self.last_error = err.abs().amax(dim=(1, 2))
+        self.F[self.head] = F
+        self.E[self.head] = err
+        self.head = (self.head + 1) % self.nsave
+        self.k = min(self.k + 1, self.nsave)
+        if self.k == 1:
+            return F
+        # keep the reference's oldest-first order of the stored vectors
+        idx = [(self.head - self.k + i) % self.nsave for i in range(self.k)]
+        Es = self.E[idx]  # [k, count, n, n]
+        Fs = self.F[idx]
+        m = self.k
+        Bm = torch.einsum("icpq,jcqp->cij", Es, Es)
+        count = F.shape[0]
+        B = torch.zeros((count, m + 1, m + 1), dtype=torch.float64, device=F.device)
+        B[:, -1, :] = -1
+        B[:, :, -1] = -1
+        B[:, -1, -1] = 0
+        B[:, :m, :m] = Bm
+        b0 = torch.zeros((count, m + 1), dtype=torch.float64, device=F.device)
+        b0[:, -1] = -1
+        c = torch.linalg.solve(B, b0)
+        return torch.einsum("ci,icpq->cpq", c[:, :m], Fs)
+
+
+class BatchSCF:
+    """Restricted HF of every molecule of a BatchEngine (hartreefock_in_memory.py:7-94 semantics,
+    batched per size group).  precision: "fp64" or "mixed" (FP32 quartets below fp32_threshold
+    until every molecule's DIIS error is below fp64_tail_diis_error, then FP64)."""
+
+    def __init__(self, be: BatchEngine, precision: str = "fp64", threshold: float = 1e-12,
+                 fp32_threshold: float = 1e-4, fp64_tail_diis_error: float = 1e-5, use_graphs: bool = True):
+        self.be = be
+        self.precision = precision
+        self.threshold = threshold
+        self.fp32_threshold = fp32_threshold
+        self.tail = fp64_tail_diis_error
+        self.use_graphs = use_graphs
+        dev = be.device
+        tot = be.mat_total
+        self.S, T, V = be.one_electron()
+        self.H = T + V
+        self.D = torch.zeros(tot, dtype=torch.float64, device=dev)
+        self.F = torch.zeros_like(self.D)
+        self.Jacc = torch.zeros_like(self.D)
+        self.Kacc = torch.zeros_like(self.D)
+        self.D32 = torch.zeros(tot, dtype=torch.float32, device=dev)
+        self.lists = {"fp64": ([be.quartets(threshold)], ["fp64"])}
+        if precision != "fp64":
+            q64, q32 = be.quartets(threshold, fp32_threshold)
+            self.lists["mixed"] = ([q64, q32], ["fp64", "fp32"])
+        self.graphs: dict = {}
+        self.builds: list[str] = []
+
+    def _fock_into_F(self, mode: str) -> None:
+        be = self.be
+        lists, precs = self.lists[mode]
+        be.jk_accumulate(self.D, self.Jacc, self.Kacc, self.D32, lists, precs)
+        for g in be.groups:
+            J = be.view(self.Jacc, g)
+            K = be.view(self.Kacc, g)
+            F = be.view(self.F, g)
+            F.copy_(be.view(self.H, g) + 0.5 * (J + J.transpose(1, 2)) - 0.25 * (K + K.transpose(1, 2)))
+
+    def fock(self, mode: str) -> None:
+        """F <- H + J(D) - K(D)/2 for the whole batch (replayed from a CUDA graph)."""
+        self.builds.append(mode)
+        if not self.use_graphs:
+            self._fock_into_F(mode)
+            return
+        if mode not in self.graphs:
+            # warm up on a side stream, then capture the build once
+            s = torch.cuda.Stream(self.be.device)
+            s.wait_stream(torch.cuda.current_stream(self.be.device))
+            with torch.cuda.stream(s):
+                self._fock_into_F(mode)
+            torch.cuda.current_stream(self.be.device).wait_stream(s)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                self._fock_into_F(mode)
+            self.graphs[mode] = g
+        self.graphs[mode].replay()
+
+    def run(self, dE_threshold: float = 1e-9, rmsd_threshold: float = 1e-9, max_iter: int = 100):
+        be = self.be
+        X, Hs, Ss, diis, E0, nocc = [], [], [], [], [], []
+        for g in be.groups:
+            S = be.view(self.S, g)
+            H = be.view(self.H, g)
+            lam, L = torch.linalg.eigh(S)
+            Xg = L @ torch.diag_embed(lam ** (-0.5)) @ L.transpose(1, 2)
+            _, C0p = torch.linalg.eigh(Xg.transpose(1, 2) @ H @ Xg.transpose(1, 2))
+            C0 = Xg @ C0p
+            Co = C0[:, :, : g.nocc]
+            be.view(self.D, g).copy_(2 * Co @ Co.transpose(1, 2))
+            E0.append(torch.sum(be.view(self.D, g) * H, dim=(1, 2)))
+            X.append(Xg)
+            Hs.append(H)
+            Ss.append(S)
+            diis.append(_BatchDIIS(len(g.mols), g.nbf, be.device))
+            nocc.append(g.nocc)
+        mode = "fp64" if self.precision == "fp64" else "mixed"
+        E = E0
+        self.iterations = 0
+        for it in range(1, max_iter + 1):
+            self.iterations = it
+            self.fock(mode)
+            conv_all = True
+            switch = mode == "mixed"
+            newE = []
+            for gi, g in enumerate(be.groups):
+                F = diis[gi].extrapolate(be.view(self.F, g).clone(), be.view(self.D, g).clone(), Ss[gi])
+                if mode == "mixed" and diis[gi].last_error is not None and bool(
+                        (diis[gi].last_error >= self.tail).any()):
+                    switch = False
+                Xg = X[gi]
+                _, Cp = torch.linalg.eigh(Xg.transpose(1, 2) @ F @ Xg)
+                C = Xg @ Cp
+                Co = C[:, :, : nocc[gi]]
+                Dn = 2 * Co @ Co.transpose(1, 2)
+                En = 0.5 * torch.sum(Dn * (Hs[gi] + F), dim=(1, 2))
+                dE = (En - E[gi]).abs().max()
+                rmsd = torch.sqrt(torch.sum((Dn - be.view(self.D, g)) ** 2, dim=(1, 2))).max()
+                if not (float(dE) < dE_threshold and float(rmsd) < rmsd_threshold):
+                    conv_all = False
+                be.view(self.D, g).copy_(Dn)
+                newE.append(En)
+            E = newE
+            if switch and mode == "mixed":
+                mode = "fp64"
+                diis = [_BatchDIIS(len(g.mols), g.nbf, be.device) for g in be.groups]
+                conv_all = False
+            if conv_all and mode == "fp64":
+                break
+        # energies back in the caller's molecule order
+        Eb = torch.cat(E).cpu().numpy()
+        out = np.empty(be.nmol)
+        out[np.array(be.order)] = Eb
+        return out

@@ -66,6 +66,13 @@ static void quartet_class_l(int qc, int &la, int &lb, int &lc, int &ld) {
 // Classes with la+lb+lc+ld >= g_generic_min_l use the warp kernel.
 static int g_generic_min_l = 5;
 
+// Autotuned launch shapes per (quartet class, precision); threads 0 = default.
+struct LaunchCfg {
+    int threads;
+    long long blocks;
+};
+static LaunchCfg g_cfg[SQ_MAX_QCLASS][3] = {};
+
 static int check_common(const char *who, const sq_basis *basis, const sq_pairs *pairs, const sq_quartets *qs,
                         const double *tab) {
     if (!basis || !pairs || !qs || !tab) return set_error(SQ_ERR_ARG, "%s: NULL argument", who);
@@ -89,6 +96,13 @@ static int run_classes(const char *who, EriArgs args, const sq_quartets *qs, int
         args.nq = n;
         int la, lb, lc, ld;
         quartet_class_l(c, la, lb, lc, ld);
+        if (mode == MODE_JK && precision >= 0 && precision < 3) {
+            args.cfg_threads = g_cfg[c][precision].threads;
+            args.cfg_blocks = g_cfg[c][precision].blocks;
+        } else {
+            args.cfg_threads = 0;
+            args.cfg_blocks = 0;
+        }
         cudaError_t e;
         const int L = la + lb + lc + ld;
         eri_launcher unrolled = nullptr;
@@ -120,6 +134,15 @@ extern "C" int sq_set_option(int key, long long value) {
         return SQ_OK;
     }
     return set_error(SQ_ERR_ARG, "sq_set_option: unknown key %d", key);
+}
+
+extern "C" int sq_set_launch_config(int qclass, int precision, int threads, long long max_blocks) {
+    if (qclass < 0 || qclass >= SQ_MAX_QCLASS || precision < 0 || precision > 2)
+        return set_error(SQ_ERR_ARG, "sq_set_launch_config: bad class %d / precision %d", qclass, precision);
+    if (threads != 0 && (threads < 32 || threads > 128 || threads % 32 != 0 || max_blocks < 1))
+        return set_error(SQ_ERR_ARG, "sq_set_launch_config: threads must be 32..128 (multiple of 32), blocks >= 1");
+    g_cfg[qclass][precision] = LaunchCfg{threads, threads ? max_blocks : 0};
+    return SQ_OK;
 }
 
 extern "C" long long sq_get_option(int key) {
@@ -171,7 +194,7 @@ extern "C" int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_slot
     if (precision != SQ_FP64) {
         if (!D32 || !pairs->prim32 || !pairs->herm32 || !slots->prim32 || !slots->herm32 || !table32)
             return set_error(SQ_ERR_ARG, "sq_jk: FP32 precision needs D32, FP32 pair/slot data and table32");
-        rc = to_float((long long)basis->nbf * basis->nbf, D, D32, s);
+        rc = to_float(mat_total(*basis), D, D32, s);
         if (rc) return rc;
     }
     EriArgs a{};

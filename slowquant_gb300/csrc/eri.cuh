@@ -46,6 +46,8 @@ struct EriArgs {
     double *Kacc;
     double *V;
     double *q;
+    int cfg_threads;        // 0: built-in launch shape
+    long long cfg_blocks;
 };
 
 constexpr double kTwoPi52 = 34.98683665524972;  // 2 pi^{5/2}
@@ -361,30 +363,31 @@ __global__ void __launch_bounds__(128) eri_class_kernel(const EriArgs args) {
             else
                 D = args.D32;
             R Dab[NA][NB], Dcd[NC][ND], Dac[NA][NC], Dad[NA][ND], Dbc[NB][NC], Dbd[NB][ND];
+            const sq_basis &bs = args.basis;
 #pragma unroll
             for (int a = 0; a < NA; ++a)
 #pragma unroll
-                for (int b = 0; b < NB; ++b) Dab[a][b] = gload(D + (oa + a) * n + ob + b);
+                for (int b = 0; b < NB; ++b) Dab[a][b] = gload(D + mat_index(bs, sa, a, sb, b));
 #pragma unroll
             for (int c = 0; c < NC; ++c)
 #pragma unroll
-                for (int d = 0; d < ND; ++d) Dcd[c][d] = gload(D + (oc + c) * n + od + d);
+                for (int d = 0; d < ND; ++d) Dcd[c][d] = gload(D + mat_index(bs, sc, c, sd, d));
 #pragma unroll
             for (int a = 0; a < NA; ++a)
 #pragma unroll
-                for (int c = 0; c < NC; ++c) Dac[a][c] = gload(D + (oa + a) * n + oc + c);
+                for (int c = 0; c < NC; ++c) Dac[a][c] = gload(D + mat_index(bs, sa, a, sc, c));
 #pragma unroll
             for (int a = 0; a < NA; ++a)
 #pragma unroll
-                for (int d = 0; d < ND; ++d) Dad[a][d] = gload(D + (oa + a) * n + od + d);
+                for (int d = 0; d < ND; ++d) Dad[a][d] = gload(D + mat_index(bs, sa, a, sd, d));
 #pragma unroll
             for (int b = 0; b < NB; ++b)
 #pragma unroll
-                for (int c = 0; c < NC; ++c) Dbc[b][c] = gload(D + (ob + b) * n + oc + c);
+                for (int c = 0; c < NC; ++c) Dbc[b][c] = gload(D + mat_index(bs, sb, b, sc, c));
 #pragma unroll
             for (int b = 0; b < NB; ++b)
 #pragma unroll
-                for (int d = 0; d < ND; ++d) Dbd[b][d] = gload(D + (ob + b) * n + od + d);
+                for (int d = 0; d < ND; ++d) Dbd[b][d] = gload(D + mat_index(bs, sb, b, sd, d));
 
             R Jab[NA][NB], Jcd[NC][ND], Kac[NA][NC], Kad[NA][ND], Kbc[NB][NC], Kbd[NB][ND];
 #pragma unroll
@@ -438,27 +441,27 @@ __global__ void __launch_bounds__(128) eri_class_kernel(const EriArgs args) {
 #pragma unroll
             for (int a = 0; a < NA; ++a)
 #pragma unroll
-                for (int b = 0; b < NB; ++b) atomicAdd(J + (oa + a) * n + ob + b, to_d(wJ * Jab[a][b]));
+                for (int b = 0; b < NB; ++b) atomicAdd(J + mat_index(bs, sa, a, sb, b), to_d(wJ * Jab[a][b]));
 #pragma unroll
             for (int c = 0; c < NC; ++c)
 #pragma unroll
-                for (int d = 0; d < ND; ++d) atomicAdd(J + (oc + c) * n + od + d, to_d(wJ * Jcd[c][d]));
+                for (int d = 0; d < ND; ++d) atomicAdd(J + mat_index(bs, sc, c, sd, d), to_d(wJ * Jcd[c][d]));
 #pragma unroll
             for (int a = 0; a < NA; ++a)
 #pragma unroll
-                for (int c = 0; c < NC; ++c) atomicAdd(K + (oa + a) * n + oc + c, to_d(wK * Kac[a][c]));
+                for (int c = 0; c < NC; ++c) atomicAdd(K + mat_index(bs, sa, a, sc, c), to_d(wK * Kac[a][c]));
 #pragma unroll
             for (int b = 0; b < NB; ++b)
 #pragma unroll
-                for (int d = 0; d < ND; ++d) atomicAdd(K + (ob + b) * n + od + d, to_d(wK * Kbd[b][d]));
+                for (int d = 0; d < ND; ++d) atomicAdd(K + mat_index(bs, sb, b, sd, d), to_d(wK * Kbd[b][d]));
 #pragma unroll
             for (int a = 0; a < NA; ++a)
 #pragma unroll
-                for (int d = 0; d < ND; ++d) atomicAdd(K + (oa + a) * n + od + d, to_d(wK * Kad[a][d]));
+                for (int d = 0; d < ND; ++d) atomicAdd(K + mat_index(bs, sa, a, sd, d), to_d(wK * Kad[a][d]));
 #pragma unroll
             for (int b = 0; b < NB; ++b)
 #pragma unroll
-                for (int c = 0; c < NC; ++c) atomicAdd(K + (ob + b) * n + oc + c, to_d(wK * Kbc[b][c]));
+                for (int c = 0; c < NC; ++c) atomicAdd(K + mat_index(bs, sb, b, sc, c), to_d(wK * Kbc[b][c]));
         }
     }
 }
@@ -469,11 +472,11 @@ typedef cudaError_t (*eri_launcher)(const EriArgs &args, int mode, int precision
 template <int LA, int LB, int LC, int LD>
 cudaError_t launch_eri_class(const EriArgs &args, int mode, int precision, cudaStream_t stream) {
     if (args.nq <= 0) return cudaSuccess;
-    const int threads = 128;
+    const int threads = args.cfg_threads > 0 ? args.cfg_threads : 128;
     long long blocks = (args.nq + threads - 1) / threads;
     // FP64: many blocks (FP64-bound, heavy-first order balances); FP32: about
     // two waves of persistent blocks so the shared Boys table is loaded rarely.
-    const long long cap = precision == SQ_FP64 ? 152LL * 16 * 8 : 152LL * 16;
+    const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : (precision == SQ_FP64 ? 152LL * 16 * 8 : 152LL * 16);
     if (blocks > cap) blocks = cap;
     (void)mode;  // per-thread kernels serve J/K launches only
     if (precision == SQ_FP64)
@@ -492,9 +495,9 @@ cudaError_t launch_eri_class_f32(const EriArgs &args, int mode, int precision, c
     (void)mode;
     (void)precision;
     if (args.nq <= 0) return cudaSuccess;
-    const int threads = 128;
+    const int threads = args.cfg_threads > 0 ? args.cfg_threads : 128;
     long long blocks = (args.nq + threads - 1) / threads;
-    const long long cap = 152LL * 16;
+    const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : 152LL * 16;
     if (blocks > cap) blocks = cap;
     eri_class_kernel<LA, LB, LC, LD, float, BOYS_FP64, MODE_JK><<<(int)blocks, threads, 0, stream>>>(args);
     return cudaGetLastError();

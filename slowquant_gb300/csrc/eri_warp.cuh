@@ -321,12 +321,17 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
                             const double *D = args.D;
                             const double wJ = 0.5 * m * v, wK = 0.25 * m * v;
                             double *J = args.Jacc, *K = args.Kacc;
-                            atomicAdd(J + A * n + B, wJ * gload(D + C * n + Dd));
-                            atomicAdd(J + C * n + Dd, wJ * gload(D + A * n + B));
-                            atomicAdd(K + A * n + C, wK * gload(D + B * n + Dd));
-                            atomicAdd(K + B * n + Dd, wK * gload(D + A * n + C));
-                            atomicAdd(K + A * n + Dd, wK * gload(D + B * n + C));
-                            atomicAdd(K + B * n + C, wK * gload(D + A * n + Dd));
+                            const sq_basis &bs = args.basis;
+                            const int a = ab / NB, b = ab % NB, c = cd / ND, d = cd % ND;
+                            const long long iab = mat_index(bs, sa, a, sb, b), icd = mat_index(bs, sc, c, sd, d);
+                            const long long iac = mat_index(bs, sa, a, sc, c), ibd = mat_index(bs, sb, b, sd, d);
+                            const long long iad = mat_index(bs, sa, a, sd, d), ibc = mat_index(bs, sb, b, sc, c);
+                            atomicAdd(J + iab, wJ * gload(D + icd));
+                            atomicAdd(J + icd, wJ * gload(D + iab));
+                            atomicAdd(K + iac, wK * gload(D + ibd));
+                            atomicAdd(K + ibd, wK * gload(D + iac));
+                            atomicAdd(K + iad, wK * gload(D + ibc));
+                            atomicAdd(K + ibc, wK * gload(D + iad));
                         }
                     }
                 }
@@ -344,7 +349,7 @@ inline cudaError_t launch_eri_warp(const EriArgs &args, const WarpClass &cls, in
                                    cudaStream_t stream) {
     if (args.nq <= 0) return cudaSuccess;
     long long blocks = (args.nq + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    const long long cap = 152LL * 64;
+    const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : 152LL * 64;
     if (blocks > cap) blocks = cap;
     const dim3 grid((unsigned)blocks), block(32 * kWarpsPerBlock);
 #define SQ_WARP_LAUNCH(R, B, M)                                                                                 \

@@ -246,6 +246,8 @@ __global__ void one_electron_kernel(const sq_basis basis, const double *tab, dou
     while ((s1 + 1) * (s1 + 2) / 2 <= idx) ++s1;
     while (s1 * (s1 + 1) / 2 > idx) --s1;
     const int s2 = idx - s1 * (s1 + 1) / 2;
+    // batch: shells of different molecules have no matrix element
+    if (basis.mat_base != nullptr && basis.mat_base[s1] != basis.mat_base[s2]) return;
     const int l1 = basis.l[s1], l2 = basis.l[s2];
     const int n1 = ncart(l1), n2 = ncart(l2);
     const int np1 = basis.nprim[s1], np2 = basis.nprim[s2];
@@ -288,7 +290,9 @@ __global__ void one_electron_kernel(const sq_basis basis, const double *tab, dou
             }
             if (Vm) {
                 const int L = l1 + l2;
-                for (int at = 0; at < basis.natom; ++at) {
+                const int at0 = basis.atom_begin ? basis.atom_begin[s1] : 0;
+                const int at1 = basis.atom_end ? basis.atom_end[s1] : basis.natom;
+                for (int at = at0; at < at1; ++at) {
                     double PC[3];
                     for (int d = 0; d < 3; ++d) PC[d] = Pc[d] - basis.atom_xyz[3 * at + d];
                     hermite_r_rt(L, p, PC, tab, R);
@@ -310,14 +314,12 @@ __global__ void one_electron_kernel(const sq_basis basis, const double *tab, dou
                 }
             }
         }
-    const long long n = basis.nbf;
-    const int o1 = basis.bf_off[s1], o2 = basis.bf_off[s2];
     for (int x = 0; x < n1; ++x)
         for (int y = 0; y < n2; ++y) {
-            const long long r = o1 + x, c = o2 + y;
-            if (S) S[r * n + c] = S[c * n + r] = sblk[x * n2 + y];
-            if (Tm) Tm[r * n + c] = Tm[c * n + r] = tblk[x * n2 + y];
-            if (Vm) Vm[r * n + c] = Vm[c * n + r] = vblk[x * n2 + y];
+            const long long rc = mat_index(basis, s1, x, s2, y), cr = mat_index(basis, s2, y, s1, x);
+            if (S) S[rc] = S[cr] = sblk[x * n2 + y];
+            if (Tm) Tm[rc] = Tm[cr] = tblk[x * n2 + y];
+            if (Vm) Vm[rc] = Vm[cr] = vblk[x * n2 + y];
         }
 }
 

@@ -73,6 +73,18 @@ __host__ __device__ constexpr double dfact_odd(int n) {  // (2n-1)!!
     return r;
 }
 
+// Index of matrix element (bf_off[s]+a, bf_off[t]+b): the full nbf x nbf
+// layout for one molecule, or the packed per-molecule block of a batch.
+__device__ __forceinline__ long long mat_index(const sq_basis &bs, int s, int a, int t, int b) {
+    const long long row = (long long)__ldg(bs.bf_off + s) + a, col = (long long)__ldg(bs.bf_off + t) + b;
+    if (bs.mat_base == nullptr) return row * bs.nbf + col;
+    return __ldg(bs.mat_base + s) + row * __ldg(bs.mat_ld + s) + col;
+}
+
+__host__ __device__ inline long long mat_total(const sq_basis &bs) {
+    return bs.mat_base == nullptr ? (long long)bs.nbf * bs.nbf : bs.mat_total;
+}
+
 // f32 <-> f64 conversion with integer instructions.  On GB300 the hardware
 // conversion runs at the FP64 rate (about 1/58 of FP32), so FP32 kernels that
 // hand values to FP64 code convert on the integer pipe instead.  Valid for

@@ -111,12 +111,15 @@ class IntegralEngine:
         self.t_coefs = torch.tensor(coefs, **f64)
         self.t_atom_xyz = torch.tensor(coords - self.origin, **f64).reshape(-1, 3).contiguous()
         self.t_atom_charge = torch.tensor(mol.atom_charges, **f64)
+        self.shell_atom = np.array([mol.atoms.index(s.origin_atom) for s in shells], dtype=np.int32)
+        self.t_shell_atom = torch.tensor(self.shell_atom, **i32)
         b = SqBasis()
         b.nshell, b.nbf, b.natom, b.nprim_total = self.nshell, self.nbf, len(mol.atoms), len(exps)
         b.center, b.l, b.nprim, b.prim_off, b.bf_off = (ptr(self.t_center), ptr(self.t_l), ptr(self.t_nprim),
                                                        ptr(self.t_prim_off), ptr(self.t_bf_off))
         b.exps, b.coefs = ptr(self.t_exps), ptr(self.t_coefs)
         b.atom_xyz, b.atom_charge = ptr(self.t_atom_xyz), ptr(self.t_atom_charge)
+        b.shell_atom = ptr(self.t_shell_atom)
         self.cbasis = b
 
         # Boys grid tables
@@ -417,3 +420,40 @@ class IntegralEngine:
         check(self.lib.sq_fock_build(self.nbf, ptr(H.contiguous()), ptr(Jacc), ptr(Kacc), ptr(F), None, None,
                                      self._stream()), "sq_fock_build")
         return F
+
+    # -------------------------------------------------------------- gradient
+    def nuclear_gradient(self, D: torch.Tensor, threshold: float = 1e-12) -> np.ndarray:
+        """RHF nuclear gradient dE_total/dR (natom x 3, Eh/bohr) at the converged density D.
+
+        Electronic part from the adjoint kernels (sq_grad_1e, sq_grad_2e) with
+        W = D F D / 2, F = H + J - K/2 built from D; nuclear-repulsion part on
+        the host.
+        """
+        self._require_eri()
+        D = D.to(device=self.device, dtype=torch.float64).contiguous()
+        S, T, V = self.one_electron()
+        F = self.fock(T + V, D, threshold, "fp64")
+        W = (0.5 * D @ F @ D).contiguous()
+        natom = len(self.mol.atoms)
+        grad = torch.zeros((natom, 3), dtype=torch.float64, device=self.device)
+        check(self.lib.sq_grad_1e(ctypes.byref(self.cbasis), ptr(self.tab64), ptr(D), ptr(W), ptr(grad),
+                                  self._stream()), "sq_grad_1e")
+        ql = self.quartets(threshold)
+        qs = ql.cstruct()
+        check(self.lib.sq_grad_2e(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(self.slots),
+                                  ctypes.byref(qs), ptr(self.tab64), ptr(D), ptr(grad), self._stream()),
+              "sq_grad_2e")
+        return grad.cpu().numpy() + nuclear_repulsion_gradient(self.mol)
+
+
+def nuclear_repulsion_gradient(mol: _Molecule) -> np.ndarray:
+    """d/dR_A of sum_{i<j} Z_i Z_j / R_ij."""
+    Z = mol.atom_charges
+    R = mol.atom_coordinates
+    g = np.zeros_like(R)
+    for i in range(len(Z)):
+        for j in range(len(Z)):
+            if i != j:
+                d = R[i] - R[j]
+                g[i] -= Z[i] * Z[j] * d / np.linalg.norm(d) ** 3
+    return g
