@@ -349,6 +349,22 @@ def gpu_arm(args) -> None:
     ms_e2e = time_events(torch, step_e2e, args.steps, flush)
     e2e_ms = float(np.mean(ms_e2e))
 
+    # precision threshold sweep: build time, one-build energy error at the FP64
+    # density, and the SCF energy error (mixed SCF switches to FP64 at the end)
+    Ffp = eng.fock(H, D, SCREEN, "fp64")
+    E_build64 = float(0.5 * torch.sum(D * (H + Ffp)))
+    sweep = []
+    for tau in args.tau_sweep:
+        eng.fock(H, D, SCREEN, "mixed", tau)
+        ms_tau = float(np.median(time_events(torch, lambda: eng.fock(H, D, SCREEN, "mixed", tau), 3, flush)))
+        Fm = eng.fock(H, D, SCREEN, "mixed", tau)
+        dE_build = float(0.5 * torch.sum(D * (H + Fm))) - E_build64
+        jkt = DirectJK(eng, SCREEN, "mixed", tau, 1e-5)
+        Et, _, _, _ = run_hartree_fock(S, T, V, jkt, ne, log, 1e-9, 1e-9, 100, True)
+        sweep.append({"fp32_threshold": tau, "fock_build_ms": ms_tau, "speedup_vs_fp64": ms64 / ms_tau,
+                      "dE_one_build": dE_build, "dE_scf": Et - E64,
+                      "mixed_builds": sum(1 for b in jkt.builds if b != "fp64"), "builds": len(jkt.builds)})
+
     # roofline of the dominant kernel (per-class launches timed alone)
     peak64 = fma_peak(lib, torch, _lib.SQ_FP64)
     peak32 = fma_peak(lib, torch, _lib.SQ_FP32)
@@ -398,6 +414,7 @@ def gpu_arm(args) -> None:
                      "traffic": None, "flops_per_launch": dom["flops"], "ms_per_launch": dom["ms"]},
         "roofline_fp64_build": {"flops": fl64, "ms": ms64, "achieved_tflops": fl64 / (ms64 * 1e-3) / 1e12,
                                 "peak_tflops": peak64 / 1e12, "frac": fl64 / (ms64 * 1e-3) / peak64},
+        "tau_sweep": sweep,
         "kernels_by_time": rows[:8],
         "gpu_launches": launches * args.steps,
         "clocks": clocks,
@@ -419,6 +436,103 @@ def gpu_arm(args) -> None:
         print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------- secondary workloads
+def _batch_molecules(n: int, seed: int = 256):
+    """n seeded water clusters (H2O)_k, k uniform in 1..6, 6-31G*."""
+    from slowquant_gb300 import systems
+    from slowquant_gb300.molecule import _Molecule
+
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(1, 7, n)
+    mols = []
+    for i, k in enumerate(sizes):
+        box = 9.0 * (k / 8.0) ** (1.0 / 3.0) + 1.0
+        m = _Molecule(systems.water_cluster(int(k), box, seed=1000 + i), 0, "angstrom")
+        m._set_basis_set("6-31G*")
+        mols.append(m)
+    return mols, sizes
+
+
+def batch_arm(args) -> None:
+    """Batched RHF of many small molecules: molecules/s over whole SCF runs, FP64 and mixed."""
+    import torch
+
+    from slowquant_gb300.batch import BatchEngine, BatchSCF
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    mols, sizes = _batch_molecules(args.batch_size)
+    t0 = time.time()
+    be = BatchEngine(mols)
+    torch.cuda.synchronize()
+    setup_s = time.time() - t0
+    res = {}
+    for prec in ("fp64", "mixed"):
+        t0 = time.time()
+        scf = BatchSCF(be, prec)
+        torch.cuda.synchronize()
+        prep_s = time.time() - t0
+        E = scf.run()  # warm-up run: captures the Fock-build graphs
+        steps = max(1, min(args.steps, 3))
+        t0 = time.time()
+        for _ in range(steps):
+            scf = BatchSCF(be, prec)
+            scf.graphs = {}
+            E = scf.run()
+        torch.cuda.synchronize()
+        scf_s = (time.time() - t0) / steps
+        mode = "fp64" if prec == "fp64" else "mixed"
+        ms_fock = float(np.median(time_events(torch, lambda: scf.fock(mode), 5)))
+        res[prec] = {"molecules_per_s": len(mols) / scf_s, "scf_s": scf_s, "iterations": scf.iterations,
+                     "fock_build_ms": ms_fock, "list_prep_s": round(prep_s, 2), "E": E}
+    dE = float(np.max(np.abs(res["mixed"]["E"] - res["fp64"]["E"])))
+    for r in res.values():
+        r.pop("E")
+    line = {
+        "metric": "molecules/s, batched RHF (FP64 vs mixed)", "value": res["mixed"]["molecules_per_s"],
+        "unit": "molecules/s", "n_gpus": 1, "steps": max(1, min(args.steps, 3)), "warmup": 1,
+        "ms_per_step": res["mixed"]["scf_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32 (mixed)", "data": "synthetic",
+        "config": {"workload": f"{len(mols)} water clusters (H2O)_k, k~U{{1..6}} (seed 256), 6-31G*, full RHF SCF",
+                   "total_bf": int(sum(m.number_bf for m in mols)), "waters": int(sizes.sum()),
+                   "step": "one batched SCF to convergence (dE, rmsD < 1e-9) of every molecule"},
+        "fp64": res["fp64"], "mixed": res["mixed"], "max_abs_dE_mixed_vs_fp64": dE,
+        "setup_s": round(setup_s, 2),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def gradient_arm(args) -> None:
+    """RHF nuclear gradient (SCF + adjoint gradient) timings for H24 STO-3G and n-octane cc-pVDZ."""
+    import torch
+
+    from slowquant_gb300 import systems
+    from slowquant_gb300.gradient import rhf_gradient, scf_energy
+    from slowquant_gb300.molecule import _Molecule
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    out = {}
+    for name, geom, basis in (("H24 chain STO-3G", systems.hydrogen_chain(24, seed=24), "sto-3g"),
+                              ("n-octane cc-pVDZ", systems.octane(), "cc-pvdz")):
+        m = _Molecule(geom, 0, "angstrom")
+        m._set_basis_set(basis)
+        rhf_gradient(m)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.time()
+        E, D, eng = scf_energy(m)
+        torch.cuda.synchronize()
+        t_scf = time.time() - t0
+        t0 = time.time()
+        g = eng.nuclear_gradient(D, 1e-12)
+        torch.cuda.synchronize()
+        t_grad = time.time() - t0
+        out[name] = {"nbf": m.number_bf, "scf_s": round(t_scf, 3), "gradient_s": round(t_grad, 3),
+                     "max_abs_grad": float(np.abs(g).max())}
+    line = {"metric": "RHF nuclear gradient wall time (s)", "value": out["n-octane cc-pVDZ"]["gradient_s"],
+            "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": False, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": "adjoint RHF gradient after SCF"}, "systems": out}
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -429,6 +543,11 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--waters", type=int, default=16, choices=[8, 16],
                     help="cluster size (16 is the benchmark workload; 8 for quick profiling)")
+    ap.add_argument("--workload", default="fock", choices=["fock", "batch", "gradient"],
+                    help="fock: the headline Fock-build line; batch / gradient: secondary measurements")
+    ap.add_argument("--batch-size", type=int, default=256)
+    ap.add_argument("--tau-sweep", type=float, nargs="*", default=[1e-5, 1e-4, 1e-3, 1e-2, 1e-1],
+                    help="FP32 Schwarz thresholds reported beside the headline (empty: skip)")
     args = ap.parse_args()
     global WATERS, SEED
     WATERS = SEED = args.waters
@@ -436,6 +555,10 @@ def main() -> None:
         args.warmup = 3
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload == "batch":
+        batch_arm(args)
+    elif args.workload == "gradient":
+        gradient_arm(args)
     else:
         gpu_arm(args)
 

@@ -257,6 +257,17 @@ int sq_grad_2e(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slo
 int sq_grad_1e(const sq_basis *basis, const double *table64, const double *D, const double *W, double *grad,
                void *stream);
 
+/* Batched symmetric eigensolver (replaces the per-molecule numpy eigh of the
+ * SCF step, slowquant/hartreefock/hartreefock_in_memory.py:63-66, when many
+ * molecules run at once).  Matrix i is dims[i] x dims[i] (1..128), row-major
+ * at A + offsets[i]; its eigenvalues go to W + w_offsets[i] in ascending order
+ * and the eigenvectors, as columns, to V + offsets[i].  Cyclic Jacobi, one
+ * CTA per matrix; stops when ||offdiag||_F <= tol ||A||_F or after max_sweeps
+ * sweeps.  sweeps (nullable, [nmat]) receives the sweeps used (-1: dims[i]
+ * outside 1..max_dim, matrix skipped).  max_dim = max(dims) (<= 128). */
+int sq_batched_eigh(int nmat, const long long *offsets, const int *dims, int max_dim, const double *A, double *W,
+                    double *V, const long long *w_offsets, double tol, int max_sweeps, int *sweeps, void *stream);
+
 /* Arithmetic-pipe probe (no reference counterpart): blocks x 256 threads each
  * run `iters` iterations of 8 independent FMA chains in FP64 (precision
  * SQ_FP64) or FP32 (otherwise), i.e. 16 * iters * 256 * blocks FLOPs; out

@@ -297,3 +297,52 @@ def run_hartree_fock(S, T, V, jk, number_electrons, dE_threshold=1e-9, rmsd_thre
         if abs(dE) < dE_threshold and rmsd < rmsd_threshold:
             break
     return E, C, F, D, energies
+
+
+def run_unrestricted_hartree_fock(S, T, V, jk, number_electrons_alpha, number_electrons_beta,
+                                  lumo_homo_mix_coeff=0.15, dE_threshold=1e-9, rmsd_threshold=1e-9,
+                                  max_scf_iterations=100, use_diis=True):
+    """unrestricted_hartreefock_in_memory.py:7-125; ``jk(D) -> (J, K)``.
+
+    Returns (E_elec, C_alpha, C_beta, D_alpha, D_beta, per-iteration energies).
+    """
+    na, nb = int(number_electrons_alpha), int(number_electrons_beta)
+    Hcore = T + V
+    lam, LS = np.linalg.eigh(S)
+    S_sqrt = LS @ np.diag(lam ** (-1 / 2)) @ LS.T
+    _, C0p = np.linalg.eigh(S_sqrt.T @ Hcore @ S_sqrt.T)
+    Ca0 = (S_sqrt @ C0p).T.copy()
+    Cb0 = (S_sqrt @ C0p).T.copy()
+    if na == nb:
+        h, lu = Ca0[na - 1].copy(), Ca0[na].copy()
+        x = lumo_homo_mix_coeff
+        Ca0[na - 1] = (h + x * lu) / (1 + x**2) ** 0.5
+        Ca0[na] = (-x * h + lu) / (1 + x**2) ** 0.5
+    Da0 = Ca0[:na].T @ Ca0[:na]
+    Db0 = Cb0[:nb].T @ Cb0[:nb]
+    E0 = np.einsum("ij,ij->", Da0 + Db0, Hcore)
+    diis_a = OracleDIIS(len(S)) if use_diis else None
+    diis_b = OracleDIIS(len(S)) if use_diis else None
+    energies = []
+    for _ in range(1, max_scf_iterations + 1):
+        Ja, Ka = jk(Da0)
+        Jb, Kb = jk(Db0)
+        Fa = Hcore + Ja + Jb - Ka
+        Fb = Hcore + Ja + Jb - Kb
+        if diis_a is not None:
+            Fa = diis_a.extrapolate(Fa, Da0, S)
+            Fb = diis_b.extrapolate(Fb, Db0, S)
+        _, Cpa = np.linalg.eigh(S_sqrt.T @ Fa @ S_sqrt)
+        _, Cpb = np.linalg.eigh(S_sqrt.T @ Fb @ S_sqrt)
+        Ca, Cb = S_sqrt @ Cpa, S_sqrt @ Cpb
+        Da = Ca[:, :na] @ Ca[:, :na].T
+        Db = Cb[:, :nb] @ Cb[:, :nb].T
+        E = 0.5 * np.einsum("ij,ij->", Da, Hcore + Fa) + 0.5 * np.einsum("ij,ij->", Db, Hcore + Fb)
+        dE = E - E0
+        rmsd_a = np.sum((Da - Da0) ** 2) ** 0.5
+        rmsd_b = np.sum((Db - Db0) ** 2) ** 0.5
+        energies.append(E)
+        Da0, Db0, E0 = Da, Db, E
+        if abs(dE) < dE_threshold and rmsd_a < rmsd_threshold and rmsd_b < rmsd_threshold:
+            break
+    return E, Ca, Cb, Da, Db, energies

@@ -102,6 +102,8 @@ def lib() -> ctypes.CDLL:
         L.sq_one_electron.argtypes = [ctypes.POINTER(SqBasis), _p, _p, _p, _p, _p]
         L.sq_quartets_expand.argtypes = [ctypes.c_longlong, _p, _p, _p, _p, _p, _p, ctypes.c_longlong, _p]
         L.sq_fma_probe.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _p, _p]
+        L.sq_batched_eigh.argtypes = [ctypes.c_int, _p, _p, ctypes.c_int, _p, _p, _p, _p, ctypes.c_double,
+                                      ctypes.c_int, _p, _p]
         _lib = L
     return _lib
 
@@ -110,6 +112,7 @@ EXPORTED = [
     "sq_version", "sq_last_error", "sq_set_option", "sq_get_option", "sq_set_launch_config", "sq_boys_table", "sq_boys",
     "sq_pair_prep", "sq_schwarz", "sq_eri_dense", "sq_jk", "sq_fock_build", "sq_one_electron",
     "sq_quartets_expand", "sq_fma_probe", "sq_slots_fill", "sq_jk_noalloc", "sq_grad_2e", "sq_grad_1e",
+    "sq_batched_eigh",
 ]
 
 

@@ -5,7 +5,8 @@ concatenated, shell pairs and shell quartets exist only inside a molecule, and
 the n_i x n_i matrices (D, J, K, S, T, V, F) of molecule i are packed blocks
 of one flat device buffer.  Molecules are ordered by basis size, so the
 blocks of equal-size molecules form a [count, n, n] tensor view: the SCF's
-linear algebra (DIIS, eigh) runs batched per size group, and every Fock
+linear algebra (DIIS, eigh) runs batched per size group (eigh on the
+library's one-CTA-per-matrix Jacobi kernel), and every Fock
 build of the whole batch is one launch per quartet class over all molecules'
 quartets (heavy-first order across molecules).  Setup (pairs, Schwarz,
 one-electron integrals) is also one launch each for the batch.
@@ -304,6 +305,35 @@ class BatchEngine:
                                  ptr(Kacc), _lib.PRECISIONS[prec], self._stream()), "sq_jk")
 
 
+_EIGH_MAX_N = 128
+_eigh_desc: dict = {}
+
+
+def batched_eigh(M: torch.Tensor, tol: float = 1e-15, max_sweeps: int = 40):
+    """Eigenvalues (ascending) and eigenvectors (columns) of a [B, n, n] FP64 symmetric stack.
+
+    Replaces torch/numpy eigh in the SCF step (hartreefock_in_memory.py:63-66)
+    with sq_batched_eigh, one CTA per matrix, for n <= 128.  Larger blocks use
+    torch.linalg.eigh (cuSOLVER).
+    """
+    B, n, _ = M.shape
+    if n > _EIGH_MAX_N:
+        return torch.linalg.eigh(M)
+    M = M.contiguous()
+    key = (B, n, M.device)
+    if key not in _eigh_desc:
+        dev = M.device
+        _eigh_desc[key] = (torch.arange(B, dtype=torch.int64, device=dev) * (n * n),
+                           torch.full((B,), n, dtype=torch.int32, device=dev),
+                           torch.arange(B, dtype=torch.int64, device=dev) * n)
+    offs, dims, woffs = _eigh_desc[key]
+    W = torch.empty((B, n), dtype=torch.float64, device=M.device)
+    V = torch.empty_like(M)
+    check(_lib.lib().sq_batched_eigh(B, ptr(offs), ptr(dims), n, ptr(M), ptr(W), ptr(V), ptr(woffs), tol,
+                                     max_sweeps, None, _lib.stream_handle()), "sq_batched_eigh")
+    return W, V
+
+
 class _BatchDIIS:
     """Pulay DIIS (diis.py:4-66 semantics) for a [count, n, n] group, ring buffer of 6."""
 
@@ -408,9 +438,9 @@ class BatchSCF:
         for g in be.groups:
             S = be.view(self.S, g)
             H = be.view(self.H, g)
-            lam, L = torch.linalg.eigh(S)
+            lam, L = batched_eigh(S)
             Xg = L @ torch.diag_embed(lam ** (-0.5)) @ L.transpose(1, 2)
-            _, C0p = torch.linalg.eigh(Xg.transpose(1, 2) @ H @ Xg.transpose(1, 2))
+            _, C0p = batched_eigh(Xg.transpose(1, 2) @ H @ Xg.transpose(1, 2))
             C0 = Xg @ C0p
             Co = C0[:, :, : g.nocc]
             be.view(self.D, g).copy_(2 * Co @ Co.transpose(1, 2))
@@ -435,7 +465,7 @@ class BatchSCF:
                         (diis[gi].last_error >= self.tail).any()):
                     switch = False
                 Xg = X[gi]
-                _, Cp = torch.linalg.eigh(Xg.transpose(1, 2) @ F @ Xg)
+                _, Cp = batched_eigh(Xg.transpose(1, 2) @ F @ Xg)
                 C = Xg @ Cp
                 Co = C[:, :, : nocc[gi]]
                 Dn = 2 * Co @ Co.transpose(1, 2)

@@ -1,6 +1,7 @@
-"""Restricted Hartree-Fock on the GPU: SCF loop, DIIS and the HF class.
+"""Restricted and unrestricted Hartree-Fock on the GPU: SCF loops, DIIS, the HF class.
 
-Drop-in for slowquant/hartreefock/{hartreefock_in_memory.py, diis.py,
+Drop-in for slowquant/hartreefock/{hartreefock_in_memory.py,
+unrestricted_hartreefock_in_memory.py, diis.py,
 hartreefockclass.py}: same names, arguments, iteration semantics and log lines.
 Linear algebra runs on the device in FP64 (torch: cuSOLVER eigh, cuBLAS
 products).  The two-electron part comes either from a dense ERI tensor
@@ -161,7 +162,7 @@ def run_hartree_fock(S, T, V, ERI, number_electrons: int, log, dE_threshold: flo
 
 
 class _HartreeFock:
-    """HF driver (hartreefockclass.py:14-152, restricted part).
+    """HF driver (hartreefockclass.py:14-136: RHF, UHF, spin densities and contamination).
 
     Extra knobs beyond the reference: ``direct_jk`` (default True: integral-
     direct Fock builds instead of the stored ERI tensor), ``precision``
@@ -205,3 +206,142 @@ class _HartreeFock:
         self.mo_coeff = C
         self.rdm1 = D
         self.fock_matrix = F
+
+    def run_unrestricted_hartree_fock(self) -> None:
+        """UHF (hartreefockclass.py:67-91): sets E_uhf and the alpha/beta MOs, 1-RDMs and Fock matrices."""
+        if self.direct_jk:
+            eri = DirectJK(self.int_obj.engine, self.int_obj.cauchy_schwarz_threshold, self.precision,
+                           self.fp32_schwarz_threshold, self.fp64_tail_diis_error)
+            S, T, V = self.int_obj.one_electron_device()
+        else:
+            eri = self.int_obj.electron_repulsion_tensor
+            S, T, V = (self.int_obj.overlap_matrix, self.int_obj.kinetic_energy_matrix,
+                       self.int_obj.nuclear_attraction_matrix)
+        E, Ca, Cb, Fa, Fb, Da, Db = run_unrestricted_hartree_fock(
+            S, T, V, eri, self.mol_obj.number_electrons_alpha, self.mol_obj.number_electrons_beta,
+            self.uhf_lumo_homo_mix_coeff, self.logger, self.de_threshold, self.rmsd_threshold,
+            self.max_scf_iterations, self.use_diis)
+        if self.direct_jk:
+            self.fock_builds = list(eri.builds)
+        self.E_uhf = E
+        self.mo_coeff_alpha = Ca
+        self.mo_coeff_beta = Cb
+        self.rdm1_alpha = Da
+        self.rdm1_beta = Db
+        self.fock_matrix_alpha = Fa
+        self.fock_matrix_beta = Fb
+
+    @property
+    def rdm1_charge(self) -> np.ndarray:
+        """D_alpha + D_beta (hartreefockclass.py:93-103)."""
+        return self.rdm1_alpha + self.rdm1_beta
+
+    @property
+    def rdm1_spin(self) -> np.ndarray:
+        """D_alpha - D_beta (hartreefockclass.py:105-115)."""
+        return self.rdm1_alpha - self.rdm1_beta
+
+    @property
+    def spin_contamination(self) -> float:
+        """N_beta - sum_ij |C^a_ai C^b_bj S_ab|^2 over occupied i, j (hartreefockclass.py:117-136)."""
+        na = self.mol_obj.number_electrons_alpha
+        nb = self.mol_obj.number_electrons_beta
+        Sab = self.mo_coeff_alpha[:, :na].T @ np.asarray(self.int_obj.overlap_matrix) @ self.mo_coeff_beta[:, :nb]
+        return self.mol_obj.number_electrons_beta - float(np.sum(Sab**2))
+
+
+def run_unrestricted_hartree_fock(S, T, V, ERI, number_electrons_alpha: int, number_electrons_beta: int,
+                                  lumo_homo_mix_coeff: float, log, dE_threshold: float, rmsd_threshold: float,
+                                  max_scf_iterations: int, use_diis: bool = True):
+    """Unrestricted Hartree-Fock (unrestricted_hartreefock_in_memory.py:7-125).
+
+    Same start (core guess, HOMO/LUMO rotation by ``lumo_homo_mix_coeff``
+    when N_alpha == N_beta), Fock matrices F_s = H + J[D_a + D_b] - K[D_s],
+    one DIIS per spin, energy, convergence test and log lines.  ERI is a dense
+    tensor or a callable D -> (J, K) such as DirectJK; with the callable each
+    iteration runs one J/K build per spin density (J is linear in D, so
+    J[D_a] + J[D_b] is the total Coulomb matrix).  Returns
+    (E_elec, C_a, C_b, F_a, F_b, D_a, D_b) as numpy arrays.
+    """
+    device = torch.device("cuda", torch.cuda.current_device())
+    log.add_to_log(
+        f"{'Iter':^4}    {'E_UHF':^18}    {'DeltaE':^13}    {'RMS_D_alpha':^12}    {'RMS_D_beta':^12}"
+    )
+    S = _dev_tensor(S, device)
+    Hcore = _dev_tensor(T, device) + _dev_tensor(V, device)
+    if callable(ERI):
+        jk = ERI
+    else:
+        G = _dev_tensor(ERI, device)
+
+        def jk(D):
+            return torch.einsum("pqrs,sr->pq", G, D), torch.einsum("psqr,sr->pq", G, D)
+
+    na, nb = int(number_electrons_alpha), int(number_electrons_beta)
+    Lambda_S, L_S = torch.linalg.eigh(S)
+    S_sqrt = L_S @ torch.diag(Lambda_S ** (-1 / 2)) @ L_S.T
+    F0prime = S_sqrt.T @ Hcore @ S_sqrt.T
+    _, C0prime = torch.linalg.eigh(F0prime)
+    C0_alpha = (S_sqrt @ C0prime).T.clone()  # rows are MOs
+    C0_beta = (S_sqrt @ C0prime).T.clone()
+    if na == nb:
+        # break the alpha/beta symmetry by rotating HOMO and LUMO
+        c_homo = C0_alpha[na - 1].clone()
+        c_lumo = C0_alpha[na].clone()
+        x = lumo_homo_mix_coeff
+        C0_alpha[na - 1] = 1 / (1 + x**2) ** 0.5 * (c_homo + x * c_lumo)
+        C0_alpha[na] = 1 / (1 + x**2) ** 0.5 * (-x * c_homo + c_lumo)
+    C0_alpha = C0_alpha[0:na]
+    C0_beta = C0_beta[0:nb]
+    D0_alpha = C0_alpha.T @ C0_alpha
+    D0_beta = C0_beta.T @ C0_beta
+    E0 = torch.sum(D0_alpha * Hcore) + torch.sum(D0_beta * Hcore)
+    number_bf = len(S)
+    diis_alpha = DIIS(number_bf) if use_diis else None
+    diis_beta = DIIS(number_bf) if use_diis else None
+    mixed = getattr(jk, "mixed", False)
+    for iteration in range(1, max_scf_iterations + 1):
+        J_alpha, K_alpha = jk(D0_alpha)
+        J_beta, K_beta = jk(D0_beta)
+        F_alpha = Hcore + J_alpha + J_beta - K_alpha
+        F_beta = Hcore + J_beta + J_alpha - K_beta
+        if diis_alpha is not None:
+            F_alpha = diis_alpha.get_extrapolated_fock_matrix(F_alpha, D0_alpha, S)
+            F_beta = diis_beta.get_extrapolated_fock_matrix(F_beta, D0_beta, S)
+            if mixed and getattr(jk, "mixed", False):
+                errs = (diis_alpha.last_error, diis_beta.last_error)
+                if all(e is not None for e in errs) and max(errs) < jk.fp64_tail_diis_error:
+                    jk.switch_to_fp64()
+                    diis_alpha, diis_beta = DIIS(number_bf), DIIS(number_bf)
+        elif mixed and getattr(jk, "mixed", False):
+            err = max(float((F @ D0 @ S - S @ D0 @ F).abs().max())
+                      for F, D0 in ((F_alpha, D0_alpha), (F_beta, D0_beta)))
+            if err < jk.fp64_tail_diis_error:
+                jk.switch_to_fp64()
+        _, Cprime_alpha = torch.linalg.eigh(S_sqrt.T @ F_alpha @ S_sqrt)
+        _, Cprime_beta = torch.linalg.eigh(S_sqrt.T @ F_beta @ S_sqrt)
+        C_alpha = S_sqrt @ Cprime_alpha
+        C_beta = S_sqrt @ Cprime_beta
+        Cocc_alpha = C_alpha[:, 0:na]
+        Cocc_beta = C_beta[:, 0:nb]
+        D_alpha = Cocc_alpha @ Cocc_alpha.T
+        D_beta = Cocc_beta @ Cocc_beta.T
+        E = 0.5 * torch.sum(D_alpha * (Hcore + F_alpha)) + 0.5 * torch.sum(D_beta * (Hcore + F_beta))
+        dE = float(E - E0)
+        rmsd_alpha = float(torch.sum((D_alpha - D0_alpha) ** 2) ** 0.5)
+        rmsd_beta = float(torch.sum((D_beta - D0_beta) ** 2) ** 0.5)
+        log.add_to_log(
+            f"{iteration:>4}    {float(E): 18.12f}    {dE: 1.6e}    {rmsd_alpha:1.6e}     {rmsd_beta:1.6e}"
+        )
+        D0_alpha, D0_beta, E0 = D_alpha, D_beta, E
+        still_mixed = mixed and getattr(jk, "mixed", False)
+        if (np.abs(dE) < dE_threshold and rmsd_alpha < rmsd_threshold and rmsd_beta < rmsd_threshold
+                and not still_mixed):
+            break
+    else:
+        log.add_to_log(
+            f"Unrestricted Hartree-Fock did not meet convergence requirements in {max_scf_iterations} iterations",
+            is_warning=True,
+        )
+    return (float(E), C_alpha.cpu().numpy(), C_beta.cpu().numpy(), F_alpha.cpu().numpy(), F_beta.cpu().numpy(),
+            D_alpha.cpu().numpy(), D_beta.cpu().numpy())

@@ -143,6 +143,36 @@ def run_system(sq, name, geom, unit, basis, *, eri=True, eri_store="full", scf=T
     return res
 
 
+def run_uhf_system(sq, name, geom, unit, basis, *, charge=0, mix=0.15, out=None):
+    """Reference UHF (unrestricted_hartreefock_in_memory.py) energy, trajectory and spin densities."""
+    t0 = time.time()
+    A = sq.SlowQuant()
+    A.set_molecule(geom, distance_unit=unit)
+    A.set_basis_set(basis)
+    A.molecule.molecular_charge = charge
+    import slowquant.hartreefock.unrestricted_hartreefock_in_memory as uhfm
+
+    log = ListLog()
+    E, Ca, Cb, Fa, Fb, Da, Db = uhfm.run_unrestricted_hartree_fock(
+        A.integral.overlap_matrix, A.integral.kinetic_energy_matrix, A.integral.nuclear_attraction_matrix,
+        A.integral.electron_repulsion_tensor, A.molecule.number_electrons_alpha,
+        A.molecule.number_electrons_beta, mix, log, 10**-9, 10**-9, 100, True,
+    )
+    iters = []
+    for line in log.lines[1:]:
+        parts = line.split()
+        if len(parts) == 5 and parts[0].isdigit():
+            iters.append(float(parts[1]))
+    res = {"basis": basis, "unit": unit, "geometry": geom, "charge": charge, "mix": mix,
+           "nbf": int(A.molecule.number_bf), "E_nuc": float(A.molecule.nuclear_repulsion),
+           "n_alpha": int(A.molecule.number_electrons_alpha), "n_beta": int(A.molecule.number_electrons_beta),
+           "E_uhf": float(E), "scf_energies": iters, "n_iter": len(iters)}
+    np.savez_compressed(os.path.join(out, f"{name}.npz"), D_alpha=Da, D_beta=Db)
+    res["seconds"] = round(time.time() - t0, 2)
+    print(name, E, res["nbf"], res["seconds"], flush=True)
+    return res
+
+
 def boys_grid(ref_boys) -> dict:
     zs = np.concatenate([
         [0.0, 1e-12, 9.9e-11, 1.1e-10, 1e-8, 1e-6, 1e-4, 1e-3, 0.01],
@@ -212,6 +242,19 @@ def main() -> None:
     for name, geom, unit, basis, kw in systems:
         if want(name):
             energies[name] = run_system(sq, name, geom, unit, basis, out=out, **kw)
+            json.dump(energies, open(energies_path, "w"), indent=1)
+    # UHF known-answer cases of the reference (tests/test_unrestrictedhartreefock.py)
+    n2 = """N   0.000000000000  0.000000000000   0.000000000000;
+                      N  2.074000000000   0.000000000000  -0.000000000000"""
+    uhf_systems = [
+        ("uhf_h2o_sto3g_mix0", H2O_CRAWFORD_BOHR, "bohr", "sto-3g", dict(mix=0.0)),
+        ("uhf_n2_631gs", n2, "bohr", "6-31G*", {}),
+        ("uhf_n2cation_631gs", n2, "bohr", "6-31G*", dict(charge=1)),
+        ("uhf_li_631gss", "Li   0.000000000000  0.000000000000   0.000000000000;", "bohr", "6-31G**", {}),
+    ]
+    for name, geom, unit, basis, kw in uhf_systems:
+        if want(name):
+            energies[name] = run_uhf_system(sq, name, geom, unit, basis, out=out, **kw)
             json.dump(energies, open(energies_path, "w"), indent=1)
 
 

@@ -69,3 +69,56 @@ def test_batch_mixed_precision(gpu_lib):
     Em = scf.run()
     assert scf.builds[0] == "mixed" and scf.builds[-1] == "fp64"
     assert np.max(np.abs(Em - E64)) < 1e-6
+
+
+def test_batched_eigh_ragged_matches_numpy(gpu_lib):
+    """sq_batched_eigh on matrices of mixed sizes (1..128) against numpy eigh."""
+    import torch
+
+    from slowquant_gb300 import _lib
+
+    rng = np.random.default_rng(3)
+    dims = [1, 2, 7, 19, 38, 57, 114, 128]
+    offs = np.concatenate([[0], np.cumsum([d * d for d in dims])[:-1]]).astype(np.int64)
+    woff = np.concatenate([[0], np.cumsum(dims)[:-1]]).astype(np.int64)
+    mats = []
+    for d in dims:
+        M = rng.normal(size=(d, d))
+        mats.append((M + M.T) / 2)
+    A = torch.tensor(np.concatenate([m.ravel() for m in mats]), dtype=torch.float64, device="cuda")
+    V = torch.zeros_like(A)
+    W = torch.zeros(sum(dims), dtype=torch.float64, device="cuda")
+    # every argument tensor stays referenced until the results are read back
+    t_off = torch.tensor(offs, device="cuda")
+    t_dims = torch.tensor(np.array(dims, np.int32), device="cuda")
+    t_woff = torch.tensor(woff, device="cuda")
+    sweeps = torch.zeros(len(dims), dtype=torch.int32, device="cuda")
+    _lib.check(_lib.lib().sq_batched_eigh(len(dims), t_off.data_ptr(), t_dims.data_ptr(), max(dims), A.data_ptr(),
+                                          W.data_ptr(), V.data_ptr(), t_woff.data_ptr(), 1e-15, 40,
+                                          sweeps.data_ptr(), _lib.stream_handle()), "sq_batched_eigh")
+    torch.cuda.synchronize()
+    Wh, Vh, sw = W.cpu().numpy(), V.cpu().numpy(), sweeps.cpu().numpy()
+    assert np.all(sw >= 0) and np.all(sw < 40)
+    for i, d in enumerate(dims):
+        w = Wh[woff[i]:woff[i] + d]
+        v = Vh[offs[i]:offs[i] + d * d].reshape(d, d)
+        wr = np.linalg.eigvalsh(mats[i])
+        np.testing.assert_allclose(w, wr, atol=1e-12 * max(1.0, np.abs(wr).max()))
+        # eigenvector residual and orthonormality
+        np.testing.assert_allclose(mats[i] @ v, v * w[None, :], atol=1e-11)
+        np.testing.assert_allclose(v.T @ v, np.eye(d), atol=1e-12)
+
+
+def test_batched_eigh_helper_uniform_stack(gpu_lib):
+    import torch
+
+    from slowquant_gb300.batch import batched_eigh
+
+    rng = np.random.default_rng(5)
+    M = rng.normal(size=(16, 66, 66))
+    M = (M + M.transpose(0, 2, 1)) / 2
+    Mt = torch.tensor(M, device="cuda")
+    W, V = batched_eigh(Mt)
+    W, V = W.cpu().numpy(), V.cpu().numpy()
+    np.testing.assert_allclose(W, np.linalg.eigvalsh(M), atol=1e-12)
+    np.testing.assert_allclose(M @ V, V * W[:, None, :], atol=1e-11)

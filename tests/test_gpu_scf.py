@@ -75,3 +75,64 @@ def test_mixed_precision_energy(gpu_lib):
         builds = A.hartree_fock.fock_builds
         assert builds[0] != "fp64" and builds[-1] == "fp64"
         assert abs(A.hartree_fock.E_hf - ref) < 1e-6
+
+
+UHF_KNOWN = {  # E_uhf + E_nuc from the reference's tests/test_unrestrictedhartreefock.py
+    "uhf_n2_631gs": (-108.942686389118, 1e-6),
+    "uhf_n2cation_631gs": (-108.36597, 1e-5),
+    "uhf_li_631gss": (-7.4313707537, 1e-5),
+}
+
+
+def _run_uhf(e, **kw):
+    import slowquant_gb300.SlowQuant as sq
+
+    A = sq.SlowQuant()
+    A.set_molecule(e["geometry"], distance_unit=e["unit"])
+    A.set_basis_set(e["basis"])
+    A.molecule.molecular_charge = e["charge"]
+    A.init_hartree_fock()
+    A.hartree_fock.logger.print_output = False
+    A.hartree_fock.uhf_lumo_homo_mix_coeff = e["mix"]
+    for k, v in kw.items():
+        setattr(A.hartree_fock, k, v)
+    A.hartree_fock.run_unrestricted_hartree_fock()
+    return A
+
+
+@pytest.mark.parametrize("name", ["uhf_h2o_sto3g_mix0", "uhf_n2_631gs", "uhf_n2cation_631gs", "uhf_li_631gss"])
+def test_uhf_energy_direct(name, gpu_lib, golden_energies):
+    from tests.conftest import load_golden
+
+    e = golden_energies[name]
+    d = load_golden(name)
+    A = _run_uhf(e)
+    hf = A.hartree_fock
+    assert abs(hf.E_uhf - e["E_uhf"]) < 1e-8
+    np.testing.assert_allclose(hf.rdm1_alpha, d["D_alpha"], atol=1e-6)
+    np.testing.assert_allclose(hf.rdm1_beta, d["D_beta"], atol=1e-6)
+    np.testing.assert_allclose(hf.rdm1_charge, d["D_alpha"] + d["D_beta"], atol=2e-6)
+    np.testing.assert_allclose(hf.rdm1_spin, d["D_alpha"] - d["D_beta"], atol=2e-6)
+    if name in UHF_KNOWN:
+        ref, tol = UHF_KNOWN[name]
+        assert abs(hf.E_uhf + A.molecule.nuclear_repulsion - ref) < tol
+    # <S^2> contamination is non-negative; zero for the closed-shell solutions
+    assert hf.spin_contamination > -1e-8
+    if name in ("uhf_h2o_sto3g_mix0", "uhf_n2_631gs"):
+        assert abs(hf.spin_contamination) < 1e-6
+
+
+def test_uhf_equals_rhf_closed_shell_and_stored_tensor(gpu_lib, golden_energies):
+    e = golden_energies["uhf_h2o_sto3g_mix0"]
+    A = _run_uhf(e, direct_jk=False)
+    A.hartree_fock.run_restricted_hartree_fock()
+    assert abs(A.hartree_fock.E_uhf - e["E_uhf"]) < 1e-8
+    assert abs(A.hartree_fock.E_hf - A.hartree_fock.E_uhf) < 1e-6
+
+
+def test_uhf_mixed_precision(gpu_lib, golden_energies):
+    e = golden_energies["uhf_n2cation_631gs"]
+    A = _run_uhf(e, precision="mixed", fp32_schwarz_threshold=1e-4)
+    builds = A.hartree_fock.fock_builds
+    assert builds[0] == "mixed" and builds[-1] == "fp64"
+    assert abs(A.hartree_fock.E_uhf - e["E_uhf"]) < 1e-6

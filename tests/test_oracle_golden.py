@@ -97,3 +97,33 @@ def test_oracle_faithful_mode_identical():
 def test_reference_known_answers(name, ref, golden_energies):
     """The reference suite's literature energies (1e-6 Eh) hold for its own output."""
     assert abs(golden_energies[name]["E_hf"] - ref) < 1e-6
+
+
+UHF_KNOWN = {  # E_uhf + E_nuc from the reference's tests/test_unrestrictedhartreefock.py
+    "uhf_n2_631gs": (-108.942686389118, 1e-6),
+    "uhf_n2cation_631gs": (-108.36597, 1e-5),
+    "uhf_li_631gss": (-7.4313707537, 1e-5),
+}
+
+
+@pytest.mark.parametrize("name", ["uhf_h2o_sto3g_mix0", "uhf_n2_631gs", "uhf_n2cation_631gs", "uhf_li_631gss"])
+def test_oracle_uhf_matches_reference(name):
+    import json
+    import os
+
+    e = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden_energies.json")))[name]
+    d = load_golden(name)
+    m = O.OracleMolecule(e["geometry"], e["basis"], e["unit"], charge=e["charge"])
+    assert m.nbf == e["nbf"]
+    V = m.eri_dense(1e-12)
+    S, T, Vn = m.one_electron()
+    E, Ca, Cb, Da, Db, its = O.run_unrestricted_hartree_fock(
+        S, T, Vn, lambda Dm: O.jk_from_eri(V, Dm), e["n_alpha"], e["n_beta"], e["mix"])
+    # both SCFs stop at |dE| < 1e-9: open-shell end points agree to a few 1e-9
+    assert abs(E - e["E_uhf"]) < 1e-8
+    np.testing.assert_allclose(its[:4], e["scf_energies"][:4], atol=1e-9)
+    np.testing.assert_allclose(Da, d["D_alpha"], atol=1e-6)
+    np.testing.assert_allclose(Db, d["D_beta"], atol=1e-6)
+    if name in UHF_KNOWN:
+        ref, tol = UHF_KNOWN[name]
+        assert abs(E + m.nuclear_repulsion - ref) < tol
