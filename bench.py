@@ -134,25 +134,40 @@ def fma_peak(lib, torch, precision: int) -> float:
     return best
 
 
-def class_work(eng, ql) -> dict:
-    """Per quartet class: contracted quartets, primitive quartets, model FLOPs."""
+def class_work(eng, ql, precision: str = "fp64") -> dict:
+    """Per quartet class: contracted quartets, primitive quartets, model FLOPs.
+
+    Primitive quartets are the ones the launch computes: the per-thread class
+    kernels (classes 0-11, and 12-18 in FP32) loop over the slots' screened
+    primitive pairs, the generic warp kernel over all of a pair's primitives.
+    """
     import torch
 
     from slowquant_gb300 import flops
 
     # quartet entries are slot ids: primitive pairs per slot
-    npp = torch.tensor(eng.pair_np[eng.slot_pair], dtype=torch.int64, device=eng.device)
+    npp_slot = torch.tensor(eng.slot_npp, dtype=torch.int64, device=eng.device)
+    npp_all = torch.tensor(eng.pair_np[eng.slot_pair], dtype=torch.int64, device=eng.device)
+    sub = torch.tensor(eng.slot_sub, dtype=torch.int64, device=eng.device)
+    # the warp kernel's share of a sub-slot: its chunk of all the pair's primitive pairs
+    S = torch.clamp(sub & 0xFFFF, min=1)
+    kk = sub >> 16
+    npp_all = (npp_all * (kk + 1)) // S - (npp_all * kk) // S
     out = {}
     for c in range(21):
         a, b = int(ql.class_off[c]), int(ql.class_off[c + 1])
         if b == a:
             continue
+        per_thread = c < 12 or (precision != "fp64" and c <= 18)
+        npp = npp_slot if per_thread else npp_all
         seg = ql.pairs[a:b].long()
         nprim = int((npp[seg[:, 0]] * npp[seg[:, 1]]).sum())
+        nuniq = int(((sub[seg[:, 0]] >> 16) == 0).sum())
         la, lb, lc, ld = flops.quartet_class_l(c)
-        f = nprim * flops.flops_per_primitive_quartet(la, lb, lc, ld) + (b - a) * flops.flops_per_contracted_quartet_jk(
+        f = nprim * flops.flops_per_primitive_quartet(la, lb, lc, ld) + nuniq * flops.flops_per_contracted_quartet_jk(
             la, lb, lc, ld)
-        out[c] = {"quartets": b - a, "prim_quartets": nprim, "flops": float(f), "class": f"{la}{lb}{lc}{ld}"}
+        out[c] = {"quartets": nuniq, "list_entries": b - a, "prim_quartets": nprim, "flops": float(f),
+                  "class": f"{la}{lb}{lc}{ld}"}
     return out
 
 
@@ -266,6 +281,8 @@ def gpu_arm(args) -> None:
     if world > 1:
         dist.init_process_group("nccl")
     lib = _lib.lib()
+    if args.jk_streams:
+        _lib.check(lib.sq_set_option(_lib.SQ_OPT_JK_STREAMS, args.jk_streams), "sq_set_option")
 
     geom = workload_geometry()
     mol = _Molecule(geom, 0, "angstrom")
@@ -274,6 +291,9 @@ def gpu_arm(args) -> None:
     eng = IntegralEngine(mol)
     q_all = eng.quartets(SCREEN)
     q64, q32 = eng.quartets(SCREEN, FP32_THR)
+    # unique contracted quartets (the J/K lists split the heaviest ones into chunks)
+    nq_unique = eng.quartets(SCREEN, split=False).nquartet
+    n64_unique, n32_unique = (x.nquartet for x in eng.quartets(SCREEN, FP32_THR, split=False))
     S, T, V = eng.one_electron()
     H = T + V
     torch.cuda.synchronize()
@@ -330,7 +350,7 @@ def gpu_arm(args) -> None:
         tot_mixed = float(t.item())
 
     ms_step = tot_mixed / args.steps
-    nq = q_all.nquartet
+    nq = nq_unique
     value = world * nq / (ms_step * 1e-3)
     ms64 = float(np.median(ms_fp64))
 
@@ -369,13 +389,13 @@ def gpu_arm(args) -> None:
     peak64 = fma_peak(lib, torch, _lib.SQ_FP64)
     peak32 = fma_peak(lib, torch, _lib.SQ_FP32)
     work64 = class_work(eng, q64)
-    work32 = class_work(eng, q32)
+    work32 = class_work(eng, q32, "fp32")
     work_all = class_work(eng, q_all)
     rows = []
     for lst, prec, work in ((q64, "fp64", work64), (q32, "fp32", work32)):
         for c, w in work.items():
             off = np.zeros(22, dtype=np.int64)
-            off[c + 1:] = w["quartets"]
+            off[c + 1:] = w["list_entries"]
             sub = QuartetList(lst.pairs[lst.class_off[c]:lst.class_off[c + 1]], off)
             eng.jk_accumulate(D, [sub], [prec])
             t = float(np.median(time_events(torch, lambda: eng.jk_accumulate(D, [sub], [prec]), 3, flush)))
@@ -395,8 +415,8 @@ def gpu_arm(args) -> None:
         "metric": METRIC, "value": value, "unit": "quartets/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64+f32 (mixed)", "data": "synthetic",
-        "config": config({"nbf": eng.nbf, "surviving_quartets": nq, "fp64_quartets": q64.nquartet,
-                          "fp32_quartets": q32.nquartet}),
+        "config": config({"nbf": eng.nbf, "surviving_quartets": nq, "fp64_quartets": n64_unique,
+                          "fp32_quartets": n32_unique, "list_entries_after_split": q_all.nquartet}),
         "fock_build_ms": {"mixed": ms_step, "fp64": ms64, "speedup_mixed_vs_fp64": ms64 / ms_step},
         "quartets_per_s": {"mixed": nq / (ms_step * 1e-3), "fp64": nq / (ms64 * 1e-3)},
         "energy": {"E_hf_fp64": E64, "E_hf_mixed": Em, "abs_dE_mixed_vs_fp64": abs(Em - E64),
@@ -421,6 +441,7 @@ def gpu_arm(args) -> None:
         "setup_s": round(setup_s, 2),
         "wall_timed_s": round(wall_mixed, 3),
         "hbm_peak_gbs": measured_peaks().get("hbm_gbs"),
+        "jk_streams": int(lib.sq_get_option(_lib.SQ_OPT_JK_STREAMS)),
     }
     if rank == 0 and not args.no_cpu:
         pairs_host = (eng.pair_shells[eng.slot_pair], q_all.pairs[: q_all.nquartet].cpu().numpy())
@@ -546,6 +567,7 @@ def main() -> None:
     ap.add_argument("--workload", default="fock", choices=["fock", "batch", "gradient"],
                     help="fock: the headline Fock-build line; batch / gradient: secondary measurements")
     ap.add_argument("--batch-size", type=int, default=256)
+    ap.add_argument("--jk-streams", type=int, default=0, help="J/K class launch streams (0: library default)")
     ap.add_argument("--tau-sweep", type=float, nargs="*", default=[1e-5, 1e-4, 1e-3, 1e-2, 1e-1],
                     help="FP32 Schwarz thresholds reported beside the headline (empty: skip)")
     args = ap.parse_args()

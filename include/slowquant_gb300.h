@@ -120,6 +120,18 @@ typedef struct sq_slots {
     double *herm;              /* [nherm_total] */
     float *prim32;             /* optional FP32 copies (NULL: not written) */
     float *herm32;
+    /* optional primitive-pair selection (NULL: the first npp[s] primitive pairs
+     * of the pair): primitive k of slot s is primitive pair
+     * prim_src[prim_src_off[s] + k] of the pair's table (i * nprim_b + j). */
+    const int *prim_src;
+    const long long *prim_src_off; /* [nslot] */
+    /* optional sub-slots (NULL: every slot is whole).  sub[s] = 0 for a whole
+     * slot; (k << 16) | S for chunk k of S of a slot's primitive pairs (its
+     * npp/pbase/hbase then describe that chunk; pair[s] is the parent's pair).
+     * Only J/K quartet lists may name sub-slots, as bra entries: J and K are
+     * linear in the integrals, so the S partial quartets add up to the whole.
+     * Dense-tensor, Schwarz and gradient lists must name whole slots. */
+    const int *sub;
 } sq_slots;
 
 /* Shell-quartet work list: device array of (bra pair, ket pair) index pairs,
@@ -142,6 +154,11 @@ const char *sq_last_error(void);
  * unrolled unless the value is 0, which sends every class to the generic
  * kernel). */
 #define SQ_OPT_GENERIC_MIN_L 1
+/* SQ_OPT_JK_STREAMS: the J/K class launches of one call are spread over this
+ * many library-owned streams (1..8, default 4), forked from and joined back
+ * into the caller's stream with events, so that one class's tail overlaps the
+ * next class; 1 launches everything on the caller's stream. */
+#define SQ_OPT_JK_STREAMS 2
 int sq_set_option(int key, long long value);
 long long sq_get_option(int key);
 
@@ -203,6 +220,16 @@ int sq_eri_dense(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *s
 int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, const sq_quartets *quartets,
           const double *table64, const float *table32, const double *D, float *D32, double *Jacc, double *Kacc,
           int precision, void *stream);
+
+/* Several densities per integral evaluation (the two spin densities of
+ * unrestricted HF, slowquant/hartreefock/unrestricted_hartreefock_in_memory.py:69-74,
+ * which the reference contracts four times with the stored tensor): like
+ * sq_jk, but D, D32, Jacc and Kacc each hold nd consecutive matrices of
+ * mat_total elements (nbf*nbf without packing), and every quartet's
+ * integrals are computed once and digested into J_i, K_i for every D_i. */
+int sq_jk_multi(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, const sq_quartets *quartets,
+                const double *table64, const float *table32, int nd, const double *D, float *D32, double *Jacc,
+                double *Kacc, int precision, void *stream);
 
 /* J/K build for callers that cannot allocate device memory.  No counterpart
  * in the reference (it has no device code).  Same arguments and results as

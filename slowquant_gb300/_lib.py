@@ -26,6 +26,7 @@ SQ_FP64 = 0
 SQ_FP32 = 1
 SQ_FP32_BOYS32 = 2
 SQ_OPT_GENERIC_MIN_L = 1
+SQ_OPT_JK_STREAMS = 2
 SQ_NOALLOC_MAX_NBF = 1024
 
 PRECISIONS = {"fp64": SQ_FP64, "fp32": SQ_FP32, "fp32_boys32": SQ_FP32_BOYS32}
@@ -54,6 +55,7 @@ class SqSlots(ctypes.Structure):
         ("nslot", ctypes.c_int), ("npp_total", ctypes.c_longlong), ("nherm_total", ctypes.c_longlong),
         ("pair", _p), ("npp", _p), ("pbase", _p), ("pstride", _p), ("hbase", _p),
         ("prim", _p), ("herm", _p), ("prim32", _p), ("herm32", _p),
+        ("prim_src", _p), ("prim_src_off", _p), ("sub", _p),
     ]
 
 
@@ -92,6 +94,8 @@ def lib() -> ctypes.CDLL:
                                    ctypes.POINTER(SqQuartets), _p, _p, _p]
         L.sq_jk.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
                             ctypes.POINTER(SqQuartets), _p, _p, _p, _p, _p, _p, ctypes.c_int, _p]
+        L.sq_jk_multi.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
+                                  ctypes.POINTER(SqQuartets), _p, _p, ctypes.c_int, _p, _p, _p, _p, ctypes.c_int, _p]
         L.sq_slots_fill.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots), _p]
         L.sq_grad_2e.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
                                  ctypes.POINTER(SqQuartets), _p, _p, _p, _p]
@@ -112,7 +116,7 @@ EXPORTED = [
     "sq_version", "sq_last_error", "sq_set_option", "sq_get_option", "sq_set_launch_config", "sq_boys_table", "sq_boys",
     "sq_pair_prep", "sq_schwarz", "sq_eri_dense", "sq_jk", "sq_fock_build", "sq_one_electron",
     "sq_quartets_expand", "sq_fma_probe", "sq_slots_fill", "sq_jk_noalloc", "sq_grad_2e", "sq_grad_1e",
-    "sq_batched_eigh",
+    "sq_batched_eigh", "sq_jk_multi",
 ]
 
 

@@ -2,6 +2,8 @@
 #include <cstdarg>
 #include <cstdio>
 
+#include <mutex>
+
 #include "capi_internal.cuh"
 #include "eri.cuh"
 #include "eri_warp.cuh"
@@ -87,33 +89,98 @@ static int check_common(const char *who, const sq_basis *basis, const sq_pairs *
     return SQ_OK;
 }
 
+// J/K class launches are independent (every contribution is an atomic add),
+// so they are spread over a small pool of streams forked from and joined back
+// into the caller's stream: the tail of one class overlaps the start of the
+// next.  g_jk_streams = 1 keeps every launch on the caller's stream.
+static int g_jk_streams = 4;
+constexpr int kMaxPoolStreams = 8;
+constexpr int kMaxPoolDevices = 64;
+
+struct StreamPool {
+    bool ready = false;
+    cudaStream_t s[kMaxPoolStreams];
+    cudaEvent_t fork;
+    cudaEvent_t join[kMaxPoolStreams];
+};
+static StreamPool g_pool[kMaxPoolDevices];
+static std::mutex g_pool_mutex;
+
+// Caller holds g_pool_mutex.
+static int pool_for_current_device(StreamPool **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(SQ_ERR_CUDA, "stream pool: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxPoolDevices) return set_error(SQ_ERR_ARG, "stream pool: device %d out of range", dev);
+    StreamPool &p = g_pool[dev];
+    if (!p.ready) {
+        e = cudaEventCreateWithFlags(&p.fork, cudaEventDisableTiming);
+        for (int i = 0; i < kMaxPoolStreams && e == cudaSuccess; ++i) {
+            e = cudaStreamCreateWithFlags(&p.s[i], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p.join[i], cudaEventDisableTiming);
+        }
+        if (e != cudaSuccess) return set_error(SQ_ERR_CUDA, "stream pool: %s", cudaGetErrorString(e));
+        p.ready = true;
+    }
+    *out = &p;
+    return SQ_OK;
+}
+
+static cudaError_t launch_class(EriArgs &args, const sq_quartets *qs, int c, int mode, int precision,
+                                cudaStream_t stream) {
+    args.quartets = reinterpret_cast<const int2 *>(qs->pairs) + qs->class_off[c];
+    args.nq = qs->class_off[c + 1] - qs->class_off[c];
+    int la, lb, lc, ld;
+    quartet_class_l(c, la, lb, lc, ld);
+    if (mode == MODE_JK && precision >= 0 && precision < 3) {
+        args.cfg_threads = g_cfg[c][precision].threads;
+        args.cfg_blocks = g_cfg[c][precision].blocks;
+    } else {
+        args.cfg_threads = 0;
+        args.cfg_blocks = 0;
+    }
+    const int L = la + lb + lc + ld;
+    eri_launcher unrolled = nullptr;
+    if (mode == MODE_JK && L < g_generic_min_l) unrolled = kLaunchers[c];
+    if (mode == MODE_JK && precision == SQ_FP32 && kLaunchersF32[c] != nullptr && g_generic_min_l > 0)
+        unrolled = kLaunchersF32[c];
+    if (unrolled != nullptr) return unrolled(args, mode, precision, stream);
+    return launch_eri_warp(args, WarpClass{la, lb, lc, ld}, mode, precision, stream);
+}
+
 static int run_classes(const char *who, EriArgs args, const sq_quartets *qs, int mode, int precision,
                        cudaStream_t stream) {
-    for (int c = 0; c < SQ_MAX_QCLASS; ++c) {
-        const long long n = qs->class_off[c + 1] - qs->class_off[c];
-        if (n == 0) continue;
-        args.quartets = reinterpret_cast<const int2 *>(qs->pairs) + qs->class_off[c];
-        args.nq = n;
-        int la, lb, lc, ld;
-        quartet_class_l(c, la, lb, lc, ld);
-        if (mode == MODE_JK && precision >= 0 && precision < 3) {
-            args.cfg_threads = g_cfg[c][precision].threads;
-            args.cfg_blocks = g_cfg[c][precision].blocks;
-        } else {
-            args.cfg_threads = 0;
-            args.cfg_blocks = 0;
+    int nonempty = 0;
+    for (int c = 0; c < SQ_MAX_QCLASS; ++c) nonempty += qs->class_off[c + 1] > qs->class_off[c];
+    const int nstream = g_jk_streams < nonempty ? g_jk_streams : nonempty;
+    if (mode == MODE_JK && nstream > 1) {
+        std::lock_guard<std::mutex> lock(g_pool_mutex);
+        StreamPool *pool = nullptr;
+        int rc = pool_for_current_device(&pool);
+        if (rc) return rc;
+        cudaError_t e = cudaEventRecord(pool->fork, stream);
+        for (int i = 0; i < nstream && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(pool->s[i], pool->fork, 0);
+        int k = 0;
+        for (int c = 0; c < SQ_MAX_QCLASS && e == cudaSuccess; ++c) {
+            if (qs->class_off[c + 1] == qs->class_off[c]) continue;
+            e = launch_class(args, qs, c, mode, precision, pool->s[k++ % nstream]);
+            if (e != cudaSuccess) {
+                set_error(SQ_ERR_CUDA, "%s: class %d: %s", who, c, cudaGetErrorString(e));
+                break;
+            }
         }
-        cudaError_t e;
-        const int L = la + lb + lc + ld;
-        eri_launcher unrolled = nullptr;
-        if (mode == MODE_JK && L < g_generic_min_l) unrolled = kLaunchers[c];
-        if (mode == MODE_JK && precision == SQ_FP32 && kLaunchersF32[c] != nullptr &&
-            g_generic_min_l > 0)
-            unrolled = kLaunchersF32[c];
-        if (unrolled != nullptr)
-            e = unrolled(args, mode, precision, stream);
-        else
-            e = launch_eri_warp(args, WarpClass{la, lb, lc, ld}, mode, precision, stream);
+        // always join what was forked, so the caller's stream (or a capture) stays whole
+        for (int i = 0; i < nstream; ++i) {
+            cudaError_t ej = cudaEventRecord(pool->join[i], pool->s[i]);
+            if (ej == cudaSuccess) ej = cudaStreamWaitEvent(stream, pool->join[i], 0);
+            if (e == cudaSuccess) e = ej;
+        }
+        if (e != cudaSuccess) return set_error(SQ_ERR_CUDA, "%s: %s", who, cudaGetErrorString(e));
+        return SQ_OK;
+    }
+    for (int c = 0; c < SQ_MAX_QCLASS; ++c) {
+        if (qs->class_off[c + 1] == qs->class_off[c]) continue;
+        const cudaError_t e = launch_class(args, qs, c, mode, precision, stream);
         if (e != cudaSuccess) return set_error(SQ_ERR_CUDA, "%s: class %d: %s", who, c, cudaGetErrorString(e));
     }
     return SQ_OK;
@@ -128,6 +195,12 @@ extern "C" int sq_version(void) { return 1; }
 extern "C" const char *sq_last_error(void) { return g_err; }
 
 extern "C" int sq_set_option(int key, long long value) {
+    if (key == SQ_OPT_JK_STREAMS) {
+        if (value < 1 || value > kMaxPoolStreams)
+            return set_error(SQ_ERR_ARG, "sq_set_option: J/K streams must be 1..%d", kMaxPoolStreams);
+        g_jk_streams = (int)value;
+        return SQ_OK;
+    }
     if (key == SQ_OPT_GENERIC_MIN_L) {
         if (value < 0) return set_error(SQ_ERR_ARG, "sq_set_option: negative L");
         g_generic_min_l = (int)value;
@@ -147,6 +220,7 @@ extern "C" int sq_set_launch_config(int qclass, int precision, int threads, long
 
 extern "C" long long sq_get_option(int key) {
     if (key == SQ_OPT_GENERIC_MIN_L) return g_generic_min_l;
+    if (key == SQ_OPT_JK_STREAMS) return g_jk_streams;
     return -1;
 }
 
@@ -180,24 +254,28 @@ extern "C" int sq_eri_dense(const sq_basis *basis, const sq_pairs *pairs, const 
     return run_classes("sq_eri_dense", a, quartets, MODE_DENSE, SQ_FP64, (cudaStream_t)stream);
 }
 
-extern "C" int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots,
-                     const sq_quartets *quartets, const double *table64, const float *table32, const double *D,
-                     float *D32, double *Jacc, double *Kacc, int precision, void *stream) {
-    int rc = check_common("sq_jk", basis, pairs, quartets, table64);
+static int jk_common(const char *who, const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots,
+                     const sq_quartets *quartets, const double *table64, const float *table32, int nd,
+                     const double *D, float *D32, double *Jacc, double *Kacc, int precision, void *stream) {
+    int rc = check_common(who, basis, pairs, quartets, table64);
     if (rc) return rc;
     if (!slots || !slots->prim || !slots->herm || !slots->pair)
-        return set_error(SQ_ERR_ARG, "sq_jk: slot layout is required");
-    if (!D || !Jacc || !Kacc) return set_error(SQ_ERR_ARG, "sq_jk: D, Jacc and Kacc are required");
+        return set_error(SQ_ERR_ARG, "%s: slot layout is required", who);
+    if (!D || !Jacc || !Kacc) return set_error(SQ_ERR_ARG, "%s: D, Jacc and Kacc are required", who);
+    if (nd < 1) return set_error(SQ_ERR_ARG, "%s: nd = %d densities", who, nd);
     if (precision != SQ_FP64 && precision != SQ_FP32 && precision != SQ_FP32_BOYS32)
-        return set_error(SQ_ERR_ARG, "sq_jk: unknown precision %d", precision);
+        return set_error(SQ_ERR_ARG, "%s: unknown precision %d", who, precision);
     cudaStream_t s = (cudaStream_t)stream;
+    const long long mt = mat_total(*basis);
     if (precision != SQ_FP64) {
         if (!D32 || !pairs->prim32 || !pairs->herm32 || !slots->prim32 || !slots->herm32 || !table32)
-            return set_error(SQ_ERR_ARG, "sq_jk: FP32 precision needs D32, FP32 pair/slot data and table32");
-        rc = to_float(mat_total(*basis), D, D32, s);
+            return set_error(SQ_ERR_ARG, "%s: FP32 precision needs D32, FP32 pair/slot data and table32", who);
+        rc = to_float(mt * nd, D, D32, s);
         if (rc) return rc;
     }
     EriArgs a{};
+    a.nd = nd;
+    a.dstride = mt;
     a.basis = *basis;
     a.pairs = *pairs;
     a.tab64 = table64;
@@ -208,5 +286,19 @@ extern "C" int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_slot
     a.use_slots = 1;
     a.Jacc = Jacc;
     a.Kacc = Kacc;
-    return run_classes("sq_jk", a, quartets, MODE_JK, precision, s);
+    return run_classes(who, a, quartets, MODE_JK, precision, s);
+}
+
+extern "C" int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots,
+                     const sq_quartets *quartets, const double *table64, const float *table32, const double *D,
+                     float *D32, double *Jacc, double *Kacc, int precision, void *stream) {
+    return jk_common("sq_jk", basis, pairs, slots, quartets, table64, table32, 1, D, D32, Jacc, Kacc, precision,
+                     stream);
+}
+
+extern "C" int sq_jk_multi(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots,
+                           const sq_quartets *quartets, const double *table64, const float *table32, int nd,
+                           const double *D, float *D32, double *Jacc, double *Kacc, int precision, void *stream) {
+    return jk_common("sq_jk_multi", basis, pairs, slots, quartets, table64, table32, nd, D, D32, Jacc, Kacc,
+                     precision, stream);
 }

@@ -48,6 +48,8 @@ struct EriArgs {
     double *q;
     int cfg_threads;        // 0: built-in launch shape
     long long cfg_blocks;
+    int nd;                 // J/K: densities digested per integral (0 or 1: one)
+    long long dstride;      // elements between consecutive densities / accumulators
 };
 
 constexpr double kTwoPi52 = 34.98683665524972;  // 2 pi^{5/2}
@@ -355,13 +357,15 @@ __global__ void __launch_bounds__(128) eri_class_kernel(const EriArgs args) {
             double m = 8.0;
             if (sa == sb) m *= 0.5;
             if (sc == sd) m *= 0.5;
-            if (P == Q) m *= 0.5;
+            if (pairP == pairQ) m *= 0.5;  // bra sub-slots of a pair count as that pair
             const R wJ = R(0.5 * m), wK = R(0.25 * m);
+            const int nd = args.nd > 1 ? args.nd : 1;
+            for (int di = 0; di < nd; ++di) {
             const R *D;
             if constexpr (std::is_same<R, double>::value)
-                D = args.D;
+                D = args.D + di * args.dstride;
             else
-                D = args.D32;
+                D = args.D32 + di * args.dstride;
             R Dab[NA][NB], Dcd[NC][ND], Dac[NA][NC], Dad[NA][ND], Dbc[NB][NC], Dbd[NB][ND];
             const sq_basis &bs = args.basis;
 #pragma unroll
@@ -431,7 +435,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(const EriArgs args) {
                             Kad[a][d] = fma(v, Dbc[b][c], Kad[a][d]);
                             Kbc[b][c] = fma(v, Dad[a][d], Kbc[b][c]);
                         }
-            double *J = args.Jacc, *K = args.Kacc;
+            double *J = args.Jacc + di * args.dstride, *K = args.Kacc + di * args.dstride;
             auto to_d = [](R x) -> double {
                 if constexpr (std::is_same<R, double>::value)
                     return x;
@@ -462,6 +466,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(const EriArgs args) {
             for (int b = 0; b < NB; ++b)
 #pragma unroll
                 for (int c = 0; c < NC; ++c) atomicAdd(K + mat_index(bs, sb, b, sc, c), to_d(wK * Kbc[b][c]));
+            }  // densities
         }
     }
 }

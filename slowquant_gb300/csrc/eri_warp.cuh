@@ -138,13 +138,23 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
         const int Q = args.use_slots ? gload(args.slots.pair + pq.y) : pq.y;
         const int i0 = gload(pr.pp_off + P), i1 = gload(pr.pp_off + P + 1);
         const int k0 = gload(pr.pp_off + Q), k1 = gload(pr.pp_off + Q + 1);
+        // a bra sub-slot (chunk k of S) covers bra primitives [ib0, ib1) of the pair
+        int ib0 = i0, ib1 = i1;
+        if (args.use_slots && args.slots.sub) {
+            const int code = gload(args.slots.sub + pq.x);
+            if (code) {
+                const int S = code & 0xffff, kc = code >> 16, np = i1 - i0;
+                ib0 = i0 + (kc * np) / S;
+                ib1 = i0 + ((kc + 1) * np) / S;
+            }
+        }
         const R *hb = herm + gload(pr.herm_off + P);
         const R *hk = herm + gload(pr.herm_off + Q);
         R acc[kWarpAccMax];
 #pragma unroll
         for (int k = 0; k < kWarpAccMax; ++k) acc[k] = R(0);
 
-        for (int i = i0; i < i1; ++i) {
+        for (int i = ib0; i < ib1; ++i) {
             const R p = gload(prim + 8 * i + 0);
             const R Px = gload(prim + 8 * i + 1), Py = gload(prim + 8 * i + 2), Pz = gload(prim + 8 * i + 3);
             const R Ub = gload(prim + 8 * i + 4);
@@ -318,20 +328,23 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
                             V[((C * n + Dd) * n + B) * n + A] = v;
                             V[((Dd * n + C) * n + B) * n + A] = v;
                         } else {
-                            const double *D = args.D;
                             const double wJ = 0.5 * m * v, wK = 0.25 * m * v;
-                            double *J = args.Jacc, *K = args.Kacc;
                             const sq_basis &bs = args.basis;
                             const int a = ab / NB, b = ab % NB, c = cd / ND, d = cd % ND;
                             const long long iab = mat_index(bs, sa, a, sb, b), icd = mat_index(bs, sc, c, sd, d);
                             const long long iac = mat_index(bs, sa, a, sc, c), ibd = mat_index(bs, sb, b, sd, d);
                             const long long iad = mat_index(bs, sa, a, sd, d), ibc = mat_index(bs, sb, b, sc, c);
-                            atomicAdd(J + iab, wJ * gload(D + icd));
-                            atomicAdd(J + icd, wJ * gload(D + iab));
-                            atomicAdd(K + iac, wK * gload(D + ibd));
-                            atomicAdd(K + ibd, wK * gload(D + iac));
-                            atomicAdd(K + iad, wK * gload(D + ibc));
-                            atomicAdd(K + ibc, wK * gload(D + iad));
+                            const int nd = args.nd > 1 ? args.nd : 1;
+                            for (int di = 0; di < nd; ++di) {
+                                const double *D = args.D + di * args.dstride;
+                                double *J = args.Jacc + di * args.dstride, *K = args.Kacc + di * args.dstride;
+                                atomicAdd(J + iab, wJ * gload(D + icd));
+                                atomicAdd(J + icd, wJ * gload(D + iab));
+                                atomicAdd(K + iac, wK * gload(D + ibd));
+                                atomicAdd(K + ibd, wK * gload(D + iac));
+                                atomicAdd(K + iad, wK * gload(D + ibc));
+                                atomicAdd(K + ibc, wK * gload(D + iad));
+                            }
                         }
                     }
                 }

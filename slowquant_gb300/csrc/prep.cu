@@ -355,13 +355,14 @@ __global__ void slots_fill_kernel(const sq_basis basis, const sq_pairs pairs, sq
     const long long hsrc = pairs.herm_off[P];
     for (int k = 0; k < n; ++k) {
         const long long dst = pb + (long long)k * stride;
+        const int kk = slots.prim_src ? slots.prim_src[slots.prim_src_off[s] + k] : k;
         for (int f = 0; f < 5; ++f) {
-            const double v = pairs.prim[8 * (src + k) + f];
+            const double v = pairs.prim[8 * (src + kk) + f];
             slots.prim[f * NPP + dst] = v;
             if (slots.prim32) slots.prim32[f * NPP + dst] = (float)v;
         }
         for (int e = 0; e < E; ++e) {
-            const double v = pairs.herm[hsrc + (long long)k * E + e];
+            const double v = pairs.herm[hsrc + (long long)kk * E + e];
             const long long d = hb + ((long long)k * E + e) * stride;
             slots.herm[d] = v;
             if (slots.herm32) slots.herm32[d] = (float)v;

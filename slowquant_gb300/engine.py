@@ -16,6 +16,17 @@ to the C ABI as raw device pointers):
   Q_bra Q_ket >= threshold of electronrepulsion.py:44-49), and warps see
   uniform loop trip counts.  With a second threshold the prefix splits into an
   FP64 part (large bounds) and an FP32 part (small bounds).
+* slots: the per-thread class kernels read primitive-pair data through the
+  slot layout, which keeps only the primitive pairs that can matter: pair
+  (i, j) is dropped when its primitive Schwarz factor times the largest one
+  in the basis is below PRIM_SCREEN (far-apart tight primitives), and pairs
+  are grouped by the surviving count.
+* split quartets: one thread per contracted quartet leaves the heavy ones
+  (e.g. (ss|ss) over 8-primitive oxygen s shells: 4096 primitive quartets)
+  as a long tail.  A J/K quartet whose primitive count exceeds SPLIT_TARGET
+  is emitted S times with bra "sub-slots" that cover consecutive chunks of
+  the bra primitive pairs; J and K are linear in the integrals, so the S
+  partial epilogues add up to the full contribution.
 """
 
 from __future__ import annotations
@@ -31,6 +42,10 @@ from ._lib import SqBasis, SqPairs, SqQuartets, SqSlots, check, ptr
 from .molecule import _Molecule
 
 NCART = [1, 3, 6, 10]
+# bound on |(ij|kl)| of a primitive quartet below which primitive pair ij is left out
+PRIM_SCREEN = 1e-17
+# primitive quartets per thread above which a J/K quartet is split over its bra primitives
+SPLIT_TARGET = 512
 
 
 def herm_size(la: int, lb: int) -> int:
@@ -101,6 +116,7 @@ class IntegralEngine:
         exps = np.concatenate([s.exponents for s in shells]).astype(np.float64)
         coefs = np.concatenate([s.component_independent_coefficients() for s in shells]).astype(np.float64)
         self.nprim = nprim
+        self.prim_off_host = prim_off
         self.bf_off_host = bf_off
         self.t_center = torch.tensor(centers, **f64)
         self.t_l = torch.tensor(self.l, **i32)
@@ -169,6 +185,8 @@ class IntegralEngine:
         herm_off = np.concatenate([[0], np.cumsum(self.pair_np * hs)[:-1]]).astype(np.int64)
         nprimpair = int(pp_off[-1])
         nherm = int((self.pair_np * hs).sum())
+        self.pp_off_host = pp_off
+        self.pair_hs = hs
         if nprimpair >= 2**31:
             raise RuntimeError("too many primitive pairs for int32 indexing")
         dev = self.device
@@ -221,6 +239,91 @@ class IntegralEngine:
             self._q = q[: self.npair].cpu().numpy()
         return self._q
 
+    @property
+    def prim_q(self) -> np.ndarray:
+        """sqrt(max (ij|ij)) of every primitive pair, indexed like the pair table's
+        primitive pairs (pp_off[P] + i * nprim_b + j).
+
+        Each primitive i of shell a with coefficient c_i is one single-primitive
+        pseudo-shell; the Schwarz kernel then gives the factor of the product
+        c_i c_j g_i g_j directly, in the normalisation of the contracted pair.
+        """
+        if getattr(self, "_prim_q", None) is None:
+            self._require_eri()
+            dev = self.device
+            total = int(self.pp_off_host[-1])
+            if total == 0:
+                self._prim_q = np.zeros(0)
+                return self._prim_q
+            shell_of_prim = np.repeat(np.arange(self.nshell), self.nprim)
+            nps = len(shell_of_prim)
+            i32 = dict(dtype=torch.int32, device=dev)
+            t_center = self.t_center[torch.tensor(shell_of_prim, device=dev)].contiguous()
+            t_l = torch.tensor(self.l[shell_of_prim], **i32)
+            t_np = torch.ones(nps, **i32)
+            t_poff = torch.arange(nps, **i32)
+            t_bf = torch.zeros(nps, **i32)
+            t_satom = torch.tensor(self.shell_atom[shell_of_prim], **i32)
+            b = SqBasis()
+            b.nshell, b.nbf, b.natom, b.nprim_total = nps, self.nbf, self.cbasis.natom, nps
+            b.center, b.l, b.nprim, b.prim_off, b.bf_off = ptr(t_center), ptr(t_l), ptr(t_np), ptr(t_poff), ptr(t_bf)
+            b.exps, b.coefs = ptr(self.t_exps), ptr(self.t_coefs)
+            b.atom_xyz, b.atom_charge, b.shell_atom = ptr(self.t_atom_xyz), ptr(self.t_atom_charge), ptr(t_satom)
+            rep = np.repeat(np.arange(self.npair), self.pair_np)
+            local = np.arange(total) - self.pp_off_host[:-1][rep]
+            npb = self.pair_npb[rep]
+            sa = self.prim_off_host[self.pair_shells[rep, 0]] + local // npb
+            sb = self.prim_off_host[self.pair_shells[rep, 1]] + local % npb
+            hs = self.pair_hs[rep]
+            t_shells = torch.tensor(np.stack([sa, sb], 1).astype(np.int32), **i32)
+            t_ppoff = torch.arange(total + 1, **i32)
+            t_hoff = torch.tensor(np.concatenate([[0], np.cumsum(hs)[:-1]]).astype(np.int64), dtype=torch.int64,
+                                  device=dev)
+            t_prim = torch.empty(total * 8, dtype=torch.float64, device=dev)
+            t_herm = torch.empty(max(int(hs.sum()), 1), dtype=torch.float64, device=dev)
+            pp = SqPairs()
+            pp.npair, pp.nprimpair = total, total
+            pp.shells, pp.pp_off, pp.herm_off = ptr(t_shells), ptr(t_ppoff), ptr(t_hoff)
+            pp.prim, pp.herm = ptr(t_prim), ptr(t_herm)
+            check(self.lib.sq_pair_prep(ctypes.byref(b), ctypes.byref(pp), self._stream()), "sq_pair_prep")
+            # diagonal quartets of the pseudo pairs, grouped by class (pairs are class-sorted)
+            cls = self.pair_class[rep]
+            lists = {}
+            for pc in np.unique(cls):
+                idx = np.nonzero(cls == pc)[0].astype(np.int32)
+                lists[quartet_class(int(pc), int(pc))] = np.stack([idx, idx], axis=1)
+            ql = self._class_lists(lists)
+            q = torch.zeros(total, dtype=torch.float64, device=dev)
+            qs = ql.cstruct()
+            check(self.lib.sq_schwarz(ctypes.byref(b), ctypes.byref(pp), ctypes.byref(qs), ptr(self.tab64), ptr(q),
+                                      self._stream()), "sq_schwarz")
+            self._prim_q = q.cpu().numpy()
+        return self._prim_q
+
+    def _prim_keep(self) -> np.ndarray:
+        """Primitive pairs kept in the slot data: q_ij * max q >= PRIM_SCREEN bounds what a
+        dropped pair adds to any primitive quartet; each pair keeps at least its largest one."""
+        qp = self.prim_q
+        keep = qp * (qp.max() if len(qp) else 0.0) >= PRIM_SCREEN
+        if len(qp):
+            rep = np.repeat(np.arange(self.npair), self.pair_np)
+            # index of each pair's largest primitive factor
+            order = np.lexsort((-qp, rep))
+            first = order[np.concatenate([[0], np.cumsum(self.pair_np)[:-1]])[self.pair_np > 0]]
+            keep[first] = True
+        return keep
+
+    @property
+    def pair_npp_eff(self) -> np.ndarray:
+        """Primitive pairs of each pair that survive primitive screening."""
+        if getattr(self, "_npp_eff", None) is None:
+            keep = self._prim_keep()
+            self._keep = keep
+            self._npp_eff = np.add.reduceat(keep.astype(np.int64), self.pp_off_host[:-1]) if len(keep) else \
+                np.zeros(self.npair, np.int64)
+            self._npp_eff[self.pair_np == 0] = 0
+        return self._npp_eff
+
     def schwarz_matrix(self) -> np.ndarray:
         """(nshell, nshell) Cauchy-Schwarz matrix (get_cauchy_schwarz_matrix)."""
         cs = np.zeros((self.nshell, self.nshell))
@@ -240,7 +343,8 @@ class IntegralEngine:
 
     def _build_slots(self) -> None:
         q = self.pair_q
-        groups = screening.pair_groups(self.pair_class, self.pair_npa, self.pair_npb, q)
+        npp_eff = self.pair_npp_eff
+        groups = screening.pair_groups(self.pair_class, npp_eff, np.ones_like(npp_eff), q)
         slot_pair = np.concatenate([g[1] for g in groups]).astype(np.int32) if groups else np.zeros(0, np.int32)
         nslot = len(slot_pair)
         npp = np.zeros(nslot, np.int32)
@@ -252,7 +356,7 @@ class IntegralEngine:
         hoff = 0
         for cls, members in groups:
             n = len(members)
-            nppg = int(self.pair_np[members[0]])
+            nppg = int(npp_eff[members[0]])
             la, lb = int(self.l[self.pair_shells[members[0], 0]]), int(self.l[self.pair_shells[members[0], 1]])
             E = herm_size(la, lb)
             sl = slice(pos, pos + n)
@@ -265,9 +369,60 @@ class IntegralEngine:
             hoff += n * nppg * E
         if poff >= 2**31:
             raise RuntimeError("too many primitive pairs for int32 slot indexing")
-        self.slot_pair = slot_pair
+        # kept primitive pairs of every slot (local indices in the pair's table)
+        starts = self.pp_off_host[:-1][slot_pair]
+        lens = self.pair_np[slot_pair]
+        first = np.repeat(np.concatenate([[0], np.cumsum(lens)[:-1]]), lens)
+        gidx = np.repeat(starts, lens) + (np.arange(int(lens.sum())) - first)
+        kept = self._keep[gidx]
+        prim_src = (gidx - np.repeat(starts, lens))[kept].astype(np.int32)
+        prim_src_off = np.concatenate([[0], np.cumsum(npp)[:-1]]).astype(np.int64)
+        assert len(prim_src) == int(npp.sum())
         self.slot_of_pair = np.empty(nslot, np.int32)
         self.slot_of_pair[slot_pair] = np.arange(nslot, dtype=np.int32)
+        # sub-slots: S (a power of two) chunks of a slot's primitive pairs, for the
+        # S a quartet with the heaviest ket group can ask for; sub-slot k of S covers
+        # primitive pairs [k*n//S, (k+1)*n//S) of its parent and shares its data
+        max_np = int(npp.max()) if nslot else 0
+        self.sub_first: dict[int, np.ndarray] = {}
+        sub_pair, sub_npp, sub_pb, sub_ps, sub_hb, sub_code = [], [], [], [], [], []
+        nsub = 0
+        la_s = self.l[self.pair_shells[slot_pair, 0]] if nslot else np.zeros(0, np.int32)
+        lb_s = self.l[self.pair_shells[slot_pair, 1]] if nslot else np.zeros(0, np.int32)
+        E_s = np.array([herm_size(int(a), int(b)) for a, b in zip(la_s, lb_s)], dtype=np.int64)
+        S = 2
+        while nslot:
+            want = (npp.astype(np.int64) * max_np > SPLIT_TARGET * (S // 2)) & (npp >= S)
+            idx = np.nonzero(want)[0]
+            if len(idx) == 0:
+                break
+            first = np.full(nslot, -1, np.int64)
+            first[idx] = nslot + nsub + S * np.arange(len(idx))
+            self.sub_first[S] = first
+            k = np.tile(np.arange(S), len(idx))
+            par = np.repeat(idx, S)
+            lo = (k * npp[par]) // S
+            hi = ((k + 1) * npp[par]) // S
+            sub_pair.append(slot_pair[par])
+            sub_npp.append(hi - lo)
+            sub_pb.append(pbase[par] + lo * pstride[par])
+            sub_ps.append(pstride[par])
+            sub_hb.append(hbase[par] + lo * E_s[par] * pstride[par])
+            sub_code.append((k << 16) | S)
+            nsub += S * len(idx)
+            S *= 2
+        self.nslot_base = nslot
+        if nsub:
+            slot_pair = np.concatenate([slot_pair] + sub_pair).astype(np.int32)
+            npp = np.concatenate([npp] + sub_npp).astype(np.int32)
+            pbase = np.concatenate([pbase] + sub_pb).astype(np.int32)
+            pstride = np.concatenate([pstride] + sub_ps).astype(np.int32)
+            hbase = np.concatenate([hbase] + sub_hb).astype(np.int64)
+        sub = np.concatenate([np.zeros(self.nslot_base, np.int64)] + sub_code).astype(np.int32)
+        self.slot_sub = sub
+        self.slot_pair = slot_pair
+        self.slot_npp = npp
+        nslot = len(slot_pair)
         dev = self.device
         i32 = dict(dtype=torch.int32, device=dev)
         self.t_slot_pair = torch.tensor(slot_pair, **i32)
@@ -276,6 +431,10 @@ class IntegralEngine:
         self.t_slot_pbase = torch.tensor(pbase, **i32)
         self.t_slot_pstride = torch.tensor(pstride, **i32)
         self.t_slot_hbase = torch.tensor(hbase, dtype=torch.int64, device=dev)
+        self.t_slot_sub = torch.tensor(sub if nslot else np.zeros(1, np.int32), **i32)
+        self.t_slot_prim_src = torch.tensor(prim_src if len(prim_src) else np.zeros(1, np.int32), **i32)
+        self.t_slot_prim_src_off = torch.tensor(prim_src_off if nslot else np.zeros(1, np.int64), dtype=torch.int64,
+                                                device=dev)
         self.t_slot_prim = torch.empty(max(5 * poff, 1), dtype=torch.float64, device=dev)
         self.t_slot_herm = torch.empty(max(hoff, 1), dtype=torch.float64, device=dev)
         self.t_slot_prim32 = torch.empty(max(5 * poff, 1), dtype=torch.float32, device=dev) if self.fp32 else None
@@ -287,39 +446,74 @@ class IntegralEngine:
                                                       ptr(self.t_slot_hbase))
         s.prim, s.herm = ptr(self.t_slot_prim), ptr(self.t_slot_herm)
         s.prim32, s.herm32 = ptr(self.t_slot_prim32), ptr(self.t_slot_herm32)
+        s.prim_src, s.prim_src_off = ptr(self.t_slot_prim_src), ptr(self.t_slot_prim_src_off)
+        s.sub = ptr(self.t_slot_sub)
         self._slots = s
-        if nslot:
-            check(self.lib.sq_slots_fill(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(s),
+        if self.nslot_base:
+            # fill the parents' data only: sub-slots point into it
+            fill = SqSlots.from_buffer_copy(s)
+            fill.nslot = self.nslot_base
+            check(self.lib.sq_slots_fill(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(fill),
                                          self._stream()), "sq_slots_fill")
 
     # -------------------------------------------------------------- quartets
-    def quartets(self, threshold: float, fp32_threshold: float | None = None, q: np.ndarray | None = None):
+    def quartets(self, threshold: float, fp32_threshold: float | None = None, q: np.ndarray | None = None,
+                 split: bool = True):
         """Unique screened quartets.  Returns one QuartetList, or (fp64, fp32) lists
         when fp32_threshold is given (bound >= fp32_threshold goes to FP64).
-        ``q`` overrides the per-pair Schwarz factors (None: the engine's own)."""
-        key = (float(threshold), None if fp32_threshold is None else float(fp32_threshold))
+        ``q`` overrides the per-pair Schwarz factors (None: the engine's own).
+        ``split``: heavy quartets of the per-thread J/K classes are emitted as
+        bra sub-slot chunks (J/K lists only; dense tensors and gradients need
+        whole quartets)."""
+        key = (float(threshold), None if fp32_threshold is None else float(fp32_threshold), bool(split))
         if q is None and key in self._quartet_cache:
             return self._quartet_cache[key]
         self._require_eri()
         own = q is None
         qv = self.pair_q if own else np.asarray(q, dtype=np.float64)
-        lists, ket_list = screening.build_tasks(self.pair_class, self.pair_npa, self.pair_npb, qv, threshold,
+        npp_eff = self.pair_npp_eff
+        lists, ket_list = screening.build_tasks(self.pair_class, npp_eff, np.ones_like(npp_eff), qv, threshold,
                                                 fp32_threshold)
         self.slots  # canonical slot numbering (from the engine's own Schwarz factors)
-        out = [self._expand(t, ket_list) for t in lists]
+        # classes with per-thread kernels: 0-11 in FP64, 0-18 in FP32
+        split_max = [11, 18] if split else [-1, -1]
+        out = [self._expand(t, ket_list, split_max[li]) for li, t in enumerate(lists)]
         res = out[0] if len(out) == 1 else (out[0], out[1])
         if own:
             self._quartet_cache[key] = res
         return res
 
-    def _expand(self, tasks: dict, ket_list: np.ndarray) -> QuartetList:
-        bra, kst, cnt, toff, off = screening.flatten_tasks(tasks)
+    def _split_tasks(self, tasks: dict, ket_list: np.ndarray, split_max_class: int) -> dict:
+        """Bra slot ids of every task block, heavy blocks replaced by their sub-slot chunks."""
+        npp = self.slot_npp
+        out = {}
+        for c in range(screening.NQCLASS):
+            blocks = []
+            for m, st, n in tasks[c]:
+                slots = self.slot_of_pair[m]
+                if c <= split_max_class and len(m):
+                    cost = int(npp[slots[0]]) * int(npp[self.slot_of_pair[ket_list[st[0]]]])
+                    S = 1
+                    while cost > SPLIT_TARGET * S and (2 * S) in self.sub_first and \
+                            self.sub_first[2 * S][slots[0]] >= 0:
+                        S *= 2
+                    if S > 1:
+                        first = self.sub_first[S][slots]
+                        for k in range(S):
+                            blocks.append(((first + k).astype(np.int32), st, n))
+                        continue
+                blocks.append((slots.astype(np.int32), st, n))
+            out[c] = blocks
+        return out
+
+    def _expand(self, tasks: dict, ket_list: np.ndarray, split_max_class: int = -1) -> QuartetList:
+        bra, kst, cnt, toff, off = screening.flatten_tasks(self._split_tasks(tasks, ket_list, split_max_class))
         nq = int(off[-1])
         dev = self.device
         pairs = torch.empty((max(nq, 1), 2), dtype=torch.int32, device=dev)
         if nq:
-            # quartet entries are slot ids: map bra pair ids and the ket order
-            t_bra = torch.tensor(self.slot_of_pair[bra], dtype=torch.int32, device=dev)
+            # quartet entries are slot ids: bra slots (or sub-slots) and the ket order
+            t_bra = torch.tensor(bra, dtype=torch.int32, device=dev)
             t_kst = torch.tensor(kst, dtype=torch.int32, device=dev)
             t_cnt = torch.tensor(cnt.astype(np.int32), dtype=torch.int32, device=dev)
             t_off = torch.tensor(toff, dtype=torch.int64, device=dev)
@@ -348,11 +542,11 @@ class IntegralEngine:
         n = self.nbf
         V = torch.zeros((n, n, n, n), dtype=torch.float64, device=self.device)
         if q is None:
-            ql = self.quartets(0.0, q=np.ones(self.npair))
+            ql = self.quartets(0.0, q=np.ones(self.npair), split=False)
         elif q is self.pair_q:
-            ql = self.quartets(threshold)
+            ql = self.quartets(threshold, split=False)
         else:
-            ql = self.quartets(threshold, q=q)
+            ql = self.quartets(threshold, q=q, split=False)
         qs = ql.cstruct()
         check(self.lib.sq_eri_dense(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(self.slots),
                                     ctypes.byref(qs), ptr(self.tab64), ptr(V), self._stream()), "sq_eri_dense")
@@ -385,6 +579,32 @@ class IntegralEngine:
                                  ctypes.byref(qs), ptr(self.tab64), ptr(self.tab32), ptr(D), ptr(D32), ptr(Jacc),
                                  ptr(Kacc), _lib.PRECISIONS[prec], self._stream()), "sq_jk")
         return Jacc, Kacc
+
+    def jk_multi(self, Ds: torch.Tensor, threshold: float = 1e-12, precision: str = "fp64",
+                 fp32_threshold: float = 1e-4):
+        """J_i, K_i (symmetrised, [nd, nbf, nbf]) for a stack of densities Ds [nd, nbf, nbf],
+        with each quartet's integrals evaluated once for all of them (sq_jk_multi)."""
+        if precision == "fp64":
+            lists, precs = [self.quartets(threshold)], ["fp64"]
+        else:
+            q64, q32 = self.quartets(threshold, fp32_threshold)
+            lists = [q64, q32]
+            precs = ["fp64", "fp32" if precision == "mixed" else "fp32_boys32"]
+        Ds = Ds.to(device=self.device, dtype=torch.float64).contiguous()
+        nd = Ds.shape[0]
+        Jacc = torch.zeros_like(Ds)
+        Kacc = torch.zeros_like(Ds)
+        D32 = torch.empty(Ds.shape, dtype=torch.float32, device=self.device)
+        for ql, prec in zip(lists, precs):
+            if ql.nquartet == 0:
+                continue
+            qs = ql.cstruct()
+            check(self.lib.sq_jk_multi(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(self.slots),
+                                       ctypes.byref(qs), ptr(self.tab64), ptr(self.tab32), nd, ptr(Ds), ptr(D32),
+                                       ptr(Jacc), ptr(Kacc), _lib.PRECISIONS[prec], self._stream()), "sq_jk_multi")
+        J = 0.5 * (Jacc + Jacc.transpose(1, 2))
+        K = 0.5 * (Kacc + Kacc.transpose(1, 2))
+        return J, K
 
     def jk(self, D: torch.Tensor, threshold: float = 1e-12, precision: str = "fp64",
            fp32_threshold: float = 1e-4):
@@ -438,7 +658,7 @@ class IntegralEngine:
         grad = torch.zeros((natom, 3), dtype=torch.float64, device=self.device)
         check(self.lib.sq_grad_1e(ctypes.byref(self.cbasis), ptr(self.tab64), ptr(D), ptr(W), ptr(grad),
                                   self._stream()), "sq_grad_1e")
-        ql = self.quartets(threshold)
+        ql = self.quartets(threshold, split=False)
         qs = ql.cstruct()
         check(self.lib.sq_grad_2e(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(self.slots),
                                   ctypes.byref(qs), ptr(self.tab64), ptr(D), ptr(grad), self._stream()),

@@ -92,6 +92,11 @@ class DirectJK:
         self.builds.append(self.precision)
         return self.engine.jk(D, self.threshold, self.precision, self.fp32_threshold)
 
+    def multi(self, Ds: torch.Tensor):
+        """(J_i, K_i) for a stack of densities from one integral pass (sq_jk_multi)."""
+        self.builds.append(self.precision)
+        return self.engine.jk_multi(Ds, self.threshold, self.precision, self.fp32_threshold)
+
 
 def run_hartree_fock(S, T, V, ERI, number_electrons: int, log, dE_threshold: float, rmsd_threshold: float,
                      max_scf_iterations: int, use_diis: bool = True):
@@ -258,8 +263,9 @@ def run_unrestricted_hartree_fock(S, T, V, ERI, number_electrons_alpha: int, num
     Same start (core guess, HOMO/LUMO rotation by ``lumo_homo_mix_coeff``
     when N_alpha == N_beta), Fock matrices F_s = H + J[D_a + D_b] - K[D_s],
     one DIIS per spin, energy, convergence test and log lines.  ERI is a dense
-    tensor or a callable D -> (J, K) such as DirectJK; with the callable each
-    iteration runs one J/K build per spin density (J is linear in D, so
+    tensor or a callable D -> (J, K) such as DirectJK; DirectJK digests both
+    spin densities in one pass over the integrals (sq_jk_multi), another
+    callable is called once per spin density (J is linear in D, so
     J[D_a] + J[D_b] is the total Coulomb matrix).  Returns
     (E_elec, C_a, C_b, F_a, F_b, D_a, D_b) as numpy arrays.
     """
@@ -301,8 +307,13 @@ def run_unrestricted_hartree_fock(S, T, V, ERI, number_electrons_alpha: int, num
     diis_beta = DIIS(number_bf) if use_diis else None
     mixed = getattr(jk, "mixed", False)
     for iteration in range(1, max_scf_iterations + 1):
-        J_alpha, K_alpha = jk(D0_alpha)
-        J_beta, K_beta = jk(D0_beta)
+        if hasattr(jk, "multi"):
+            # both spin densities against one evaluation of the integrals
+            Js, Ks = jk.multi(torch.stack([D0_alpha, D0_beta]))
+            J_alpha, J_beta, K_alpha, K_beta = Js[0], Js[1], Ks[0], Ks[1]
+        else:
+            J_alpha, K_alpha = jk(D0_alpha)
+            J_beta, K_beta = jk(D0_beta)
         F_alpha = Hcore + J_alpha + J_beta - K_alpha
         F_beta = Hcore + J_beta + J_alpha - K_beta
         if diis_alpha is not None:

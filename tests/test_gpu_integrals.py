@@ -153,3 +153,102 @@ def test_driver_entry_points_follow_reference_screening():
         Vs = er.electron_repulsion_integral_driver(m, cs, thr)
         np.testing.assert_allclose(Vs, full, atol=tol)
     assert np.all(er.electron_repulsion_integral_driver(m, cs, 1e10) == 0.0)
+
+
+def test_primitive_pair_screening(monkeypatch):
+    """Dropping primitive pairs with bound q_ij * max q < 1e-17 leaves J/K unchanged (1e-11)."""
+    import torch
+
+    from slowquant_gb300 import engine as E
+    from slowquant_gb300 import systems
+
+    geom = systems.water_cluster(4, 8.0, seed=4)
+    eng = _engine(geom, "cc-pvdz", "angstrom")
+    D = torch.tensor(_random_density(eng.nbf, 2), dtype=torch.float64, device="cuda")
+    J1, K1 = (x.cpu().numpy() for x in eng.jk(D, 1e-12, "fp64"))
+    kept, total = int(eng.slot_npp[:eng.nslot_base].sum()), int(eng.pair_np.sum())
+    assert kept < total
+    # primitive Schwarz factors bound the contracted ones: q_P <= sum_ij q_ij
+    qp = eng.prim_q
+    qsum = np.add.reduceat(qp, eng.pp_off_host[:-1])
+    assert np.all(eng.pair_q <= qsum * (1 + 1e-12) + 1e-300)
+    monkeypatch.setattr(E, "PRIM_SCREEN", 0.0)
+    eng0 = _engine(geom, "cc-pvdz", "angstrom")
+    J0, K0 = (x.cpu().numpy() for x in eng0.jk(D, 1e-12, "fp64"))
+    assert int(eng0.slot_npp[:eng0.nslot_base].sum()) == total
+    np.testing.assert_allclose(J1, J0, atol=1e-11)
+    np.testing.assert_allclose(K1, K0, atol=1e-11)
+
+
+def test_split_quartets_match_whole(monkeypatch):
+    """Heavy J/K quartets split into bra sub-slot chunks give the same J/K (both kernels)."""
+    import torch
+
+    from slowquant_gb300 import _lib
+    from slowquant_gb300 import engine as E
+    from slowquant_gb300 import systems
+
+    geom = systems.water_cluster(3, 6.0, seed=3)
+    monkeypatch.setattr(E, "SPLIT_TARGET", 64)
+    eng = _engine(geom, "cc-pvdz", "angstrom")
+    D = torch.tensor(_random_density(eng.nbf, 3), dtype=torch.float64, device="cuda")
+    ql = eng.quartets(1e-12)
+    whole = eng.quartets(1e-12, split=False)
+    assert ql.nquartet > whole.nquartet  # some quartets were split
+    assert int((eng.slot_sub != 0).sum()) > 0
+    J1, K1 = (x.cpu().numpy() for x in eng.jk(D, 1e-12, "fp64"))
+    lists, precs = [whole], ["fp64"]
+    Jw, Kw = eng.jk_accumulate(D, lists, precs)
+    Jw = (0.5 * (Jw + Jw.T)).cpu().numpy()
+    Kw = (0.5 * (Kw + Kw.T)).cpu().numpy()
+    np.testing.assert_allclose(J1, Jw, atol=1e-11)
+    np.testing.assert_allclose(K1, Kw, atol=1e-11)
+    # the generic warp kernel honours sub-slots too
+    _lib.lib().sq_set_option(_lib.SQ_OPT_GENERIC_MIN_L, 0)
+    J2, K2 = (x.cpu().numpy() for x in eng.jk(D, 1e-12, "fp64"))
+    np.testing.assert_allclose(J2, Jw, atol=1e-11)
+    np.testing.assert_allclose(K2, Kw, atol=1e-11)
+    # mixed precision lists split as well (FP32 error scale)
+    J3, K3 = (x.cpu().numpy() for x in eng.jk(D, 1e-12, "mixed", fp32_threshold=1e-4))
+    assert np.max(np.abs(J3 - Jw)) < 1e-6 and np.max(np.abs(K3 - Kw)) < 1e-6
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_jk_multi_matches_single_density_builds(precision):
+    """sq_jk_multi (one integral pass, several densities) == one sq_jk per density."""
+    import torch
+
+    from slowquant_gb300 import systems
+
+    eng = _engine(systems.water_cluster(2, 5.0, seed=2), "cc-pvdz", "angstrom")
+    Ds = torch.tensor(np.stack([_random_density(eng.nbf, s) for s in (7, 8, 9)]), dtype=torch.float64,
+                      device="cuda")
+    J, K = eng.jk_multi(Ds, 1e-12, precision, 1e-4)
+    for i in range(3):
+        Ji, Ki = eng.jk(Ds[i], 1e-12, precision, 1e-4)
+        tol = 1e-11 if precision == "fp64" else 1e-9
+        np.testing.assert_allclose(J[i].cpu().numpy(), Ji.cpu().numpy(), atol=tol)
+        np.testing.assert_allclose(K[i].cpu().numpy(), Ki.cpu().numpy(), atol=tol)
+
+
+def test_jk_stream_pool_matches_single_stream():
+    """Class launches spread over the library's streams == all on the caller's stream."""
+    import torch
+
+    from slowquant_gb300 import _lib, systems
+
+    L = _lib.lib()
+    eng = _engine(systems.water_cluster(2, 5.0, seed=2), "cc-pvdz", "angstrom")
+    D = torch.tensor(_random_density(eng.nbf, 4), dtype=torch.float64, device="cuda")
+    default = L.sq_get_option(_lib.SQ_OPT_JK_STREAMS)
+    assert default >= 1
+    try:
+        _lib.check(L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, 1), "sq_set_option")
+        J1, K1 = (x.cpu().numpy() for x in eng.jk(D, 1e-12, "mixed", 1e-4))
+        _lib.check(L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, 8), "sq_set_option")
+        J8, K8 = (x.cpu().numpy() for x in eng.jk(D, 1e-12, "mixed", 1e-4))
+        assert L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, 9) != 0  # out of range is rejected
+    finally:
+        L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, default)
+    np.testing.assert_allclose(J8, J1, atol=1e-11)
+    np.testing.assert_allclose(K8, K1, atol=1e-11)

@@ -136,3 +136,23 @@ def test_uhf_mixed_precision(gpu_lib, golden_energies):
     builds = A.hartree_fock.fock_builds
     assert builds[0] == "mixed" and builds[-1] == "fp64"
     assert abs(A.hartree_fock.E_uhf - e["E_uhf"]) < 1e-6
+
+
+def test_ao_to_mo_transforms_match_einsum(gpu_lib, golden_energies):
+    """integralfunctions.py:186-211 against the reference's einsum contractions."""
+    from slowquant_gb300.integralfunctions import one_electron_integral_transform, two_electron_integral_transform
+
+    e = golden_energies["h2o_631gs"]
+    A = _run(e["geometry"], e["basis"], e["unit"])
+    C = A.hartree_fock.mo_coeff
+    h = A.integral.kinetic_energy_matrix + A.integral.nuclear_attraction_matrix
+    g = A.integral.electron_repulsion_tensor
+    h_mo = one_electron_integral_transform(C, h)
+    g_mo = two_electron_integral_transform(C, g)
+    np.testing.assert_allclose(h_mo, np.einsum("ai,bj,ab->ij", C, C, h), atol=1e-11)
+    ref = np.einsum("ai,bj,ck,dl,abcd->ijkl", C, C, C, C, g, optimize=True)
+    np.testing.assert_allclose(g_mo, ref, atol=1e-11)
+    # a rectangular (active-space) C as well
+    Ca = C[:, 2:9]
+    np.testing.assert_allclose(two_electron_integral_transform(Ca, g),
+                               np.einsum("ai,bj,ck,dl,abcd->ijkl", Ca, Ca, Ca, Ca, g, optimize=True), atol=1e-11)
