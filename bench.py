@@ -385,6 +385,12 @@ def gpu_arm(args) -> None:
                       "dE_one_build": dE_build, "dE_scf": Et - E64,
                       "mixed_builds": sum(1 for b in jkt.builds if b != "fp64"), "builds": len(jkt.builds)})
 
+    # the two halves of the mixed build, each timed alone (all its classes, stream pool)
+    ms_part = {}
+    for name, lst, prec in (("fp64_list", q64, "fp64"), ("fp32_list", q32, "fp32")):
+        eng.jk_accumulate(D, [lst], [prec])
+        ms_part[name] = float(np.median(time_events(torch, lambda: eng.jk_accumulate(D, [lst], [prec]), 5, flush)))
+
     # roofline of the dominant kernel (per-class launches timed alone)
     peak64 = fma_peak(lib, torch, _lib.SQ_FP64)
     peak32 = fma_peak(lib, torch, _lib.SQ_FP32)
@@ -417,7 +423,8 @@ def gpu_arm(args) -> None:
         "vs_baseline": None, "dtype": "f64+f32 (mixed)", "data": "synthetic",
         "config": config({"nbf": eng.nbf, "surviving_quartets": nq, "fp64_quartets": n64_unique,
                           "fp32_quartets": n32_unique, "list_entries_after_split": q_all.nquartet}),
-        "fock_build_ms": {"mixed": ms_step, "fp64": ms64, "speedup_mixed_vs_fp64": ms64 / ms_step},
+        "fock_build_ms": {"mixed": ms_step, "fp64": ms64, "speedup_mixed_vs_fp64": ms64 / ms_step,
+                          "mixed_fp64_list_alone": ms_part["fp64_list"], "mixed_fp32_list_alone": ms_part["fp32_list"]},
         "quartets_per_s": {"mixed": nq / (ms_step * 1e-3), "fp64": nq / (ms64 * 1e-3)},
         "energy": {"E_hf_fp64": E64, "E_hf_mixed": Em, "abs_dE_mixed_vs_fp64": abs(Em - E64),
                    "mixed_builds": n_mixed_builds, "total_builds_mixed": len(jkm.builds),
@@ -546,8 +553,29 @@ def gradient_arm(args) -> None:
         g = eng.nuclear_gradient(D, 1e-12)
         torch.cuda.synchronize()
         t_grad = time.time() - t0
+        # central finite differences (step 1e-4 bohr) of the FP64 GPU energy
+        from slowquant_gb300.gradient import molecule_from_coords
+        from slowquant_gb300.molecule import ANGSTROM_TO_BOHR
+
+        symbols = [a.split()[0] for a in geom.split(";") if a.strip()]
+        xyz = np.array([[float(v) * ANGSTROM_TO_BOHR for v in a.split()[1:]] for a in geom.split(";") if a.strip()])
+        if basis == "sto-3g":
+            comps = [(a, 0) for a in range(len(xyz))]
+        else:
+            comps = [(0, 0), (3, 1), (9, 2), (20, 0)]
+        h = 1e-4
+        dev = []
+        for a, d in comps:
+            xp, xm = xyz.copy(), xyz.copy()
+            xp[a, d] += h
+            xm[a, d] -= h
+            Ep = scf_energy(molecule_from_coords(symbols, xp, basis), conv=1e-11)[0]
+            Em = scf_energy(molecule_from_coords(symbols, xm, basis), conv=1e-11)[0]
+            dev.append(abs((Ep - Em) / (2 * h) - g[a, d]))
         out[name] = {"nbf": m.number_bf, "scf_s": round(t_scf, 3), "gradient_s": round(t_grad, 3),
-                     "max_abs_grad": float(np.abs(g).max())}
+                     "max_abs_grad": float(np.abs(g).max()),
+                     "fd_check": {"components": len(comps), "step_bohr": h,
+                                  "max_abs_dev_eh_per_bohr": float(max(dev))}}
     line = {"metric": "RHF nuclear gradient wall time (s)", "value": out["n-octane cc-pVDZ"]["gradient_s"],
             "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": False, "dtype": "f64",
             "data": "synthetic", "config": {"workload": "adjoint RHF gradient after SCF"}, "systems": out}

@@ -155,9 +155,11 @@ const char *sq_last_error(void);
  * kernel). */
 #define SQ_OPT_GENERIC_MIN_L 1
 /* SQ_OPT_JK_STREAMS: the J/K class launches of one call are spread over this
- * many library-owned streams (1..8, default 4), forked from and joined back
+ * many library-owned streams (1..16, default 8), forked from and joined back
  * into the caller's stream with events, so that one class's tail overlaps the
- * next class; 1 launches everything on the caller's stream. */
+ * next class; 1 launches everything on the caller's stream.  Successive calls
+ * take the next streams of a pool of 16, so calls issued concurrently from
+ * different caller streams run side by side. */
 #define SQ_OPT_JK_STREAMS 2
 int sq_set_option(int key, long long value);
 long long sq_get_option(int key);

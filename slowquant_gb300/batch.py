@@ -296,13 +296,25 @@ class BatchEngine:
                       lists, precs) -> None:
         Jacc.zero_()
         Kacc.zero_()
-        for ql, prec in zip(lists, precs):
-            if ql.nquartet == 0:
-                continue
+        work = [(ql, prec) for ql, prec in zip(lists, precs) if ql.nquartet]
+        main = torch.cuda.current_stream(self.device)
+        # lists after the first run concurrently from side streams (all only add into Jacc/Kacc);
+        # the fork/join is stream-ordered, so it also holds inside a CUDA-graph capture
+        if not hasattr(self, "_sides"):
+            self._sides = []
+        while len(self._sides) < len(work) - 1:
+            self._sides.append(torch.cuda.Stream(self.device))
+        side = self._sides[: max(len(work) - 1, 0)]
+        for s in side:
+            s.wait_stream(main)
+        for i, (ql, prec) in enumerate(work):
+            st = main if i == 0 else side[i - 1]
             qs = ql.cstruct()
             check(self.lib.sq_jk(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(self.slots),
                                  ctypes.byref(qs), ptr(self.tab64), ptr(self.tab32), ptr(D), ptr(D32), ptr(Jacc),
-                                 ptr(Kacc), _lib.PRECISIONS[prec], self._stream()), "sq_jk")
+                                 ptr(Kacc), _lib.PRECISIONS[prec], st.cuda_stream), "sq_jk")
+        for s in side:
+            main.wait_stream(s)
 
 
 _EIGH_MAX_N = 128
@@ -432,9 +444,31 @@ class BatchSCF:
             self.graphs[mode] = g
         self.graphs[mode].replay()
 
+    def _eigh_all(self, A_flat: torch.Tensor):
+        """Eigenpairs of every molecule's block of a packed buffer in one launch (sq_batched_eigh)."""
+        be = self.be
+        if not hasattr(self, "_eig_desc"):
+            dev = be.device
+            nbf = np.array(be.mol_nbf, dtype=np.int64)
+            self._eig_desc = (torch.tensor(np.array(be.mol_base, dtype=np.int64), device=dev),
+                              torch.tensor(nbf.astype(np.int32), device=dev),
+                              torch.tensor(np.concatenate([[0], np.cumsum(nbf)[:-1]]).astype(np.int64), device=dev),
+                              int(nbf.sum()), int(nbf.max()))
+        offs, dims, woffs, ntot, nmax = self._eig_desc
+        if nmax > _EIGH_MAX_N:
+            out = torch.empty_like(A_flat)
+            for g in be.groups:
+                be.view(out, g).copy_(torch.linalg.eigh(be.view(A_flat, g))[1])
+            return out
+        W = torch.empty(ntot, dtype=torch.float64, device=be.device)
+        V = torch.empty_like(A_flat)
+        check(_lib.lib().sq_batched_eigh(be.nmol, ptr(offs), ptr(dims), nmax, ptr(A_flat), ptr(W), ptr(V),
+                                         ptr(woffs), 1e-14, 40, None, _lib.stream_handle()), "sq_batched_eigh")
+        return V
+
     def run(self, dE_threshold: float = 1e-9, rmsd_threshold: float = 1e-9, max_iter: int = 100):
         be = self.be
-        X, Hs, Ss, diis, E0, nocc = [], [], [], [], [], []
+        X, Hs, Ss, diis, E0, nocc, U = [], [], [], [], [], [], []
         for g in be.groups:
             S = be.view(self.S, g)
             H = be.view(self.H, g)
@@ -442,6 +476,7 @@ class BatchSCF:
             Xg = L @ torch.diag_embed(lam ** (-0.5)) @ L.transpose(1, 2)
             _, C0p = batched_eigh(Xg.transpose(1, 2) @ H @ Xg.transpose(1, 2))
             C0 = Xg @ C0p
+            U.append(C0p)
             Co = C0[:, :, : g.nocc]
             be.view(self.D, g).copy_(2 * Co @ Co.transpose(1, 2))
             E0.append(torch.sum(be.view(self.D, g) * H, dim=(1, 2)))
@@ -453,31 +488,40 @@ class BatchSCF:
         mode = "fp64" if self.precision == "fp64" else "mixed"
         E = E0
         self.iterations = 0
+        Fp = torch.zeros_like(self.F)  # packed S^-1/2 F S^-1/2 of every molecule
+        Fx = [None] * len(be.groups)
+        ng = len(be.groups)
         for it in range(1, max_iter + 1):
             self.iterations = it
             self.fock(mode)
-            conv_all = True
-            switch = mode == "mixed"
-            newE = []
+            # per size group: DIIS and the orthogonal-basis Fock matrix
             for gi, g in enumerate(be.groups):
                 F = diis[gi].extrapolate(be.view(self.F, g).clone(), be.view(self.D, g).clone(), Ss[gi])
-                if mode == "mixed" and diis[gi].last_error is not None and bool(
-                        (diis[gi].last_error >= self.tail).any()):
-                    switch = False
-                Xg = X[gi]
-                _, Cp = batched_eigh(Xg.transpose(1, 2) @ F @ Xg)
-                C = Xg @ Cp
+                Fx[gi] = F
+                # in the previous iteration's orbital basis U the Fock matrix is nearly
+                # diagonal, so the Jacobi sweeps converge in a few sweeps
+                XU = X[gi] @ U[gi]
+                be.view(Fp, g).copy_(XU.transpose(1, 2) @ F @ XU)
+            # one eigensolver launch for all molecules
+            V = self._eigh_all(Fp)
+            stats = torch.zeros((ng, 3), dtype=torch.float64, device=be.device)
+            newE = []
+            for gi, g in enumerate(be.groups):
+                U[gi] = U[gi] @ be.view(V, g)
+                C = X[gi] @ U[gi]
                 Co = C[:, :, : nocc[gi]]
                 Dn = 2 * Co @ Co.transpose(1, 2)
-                En = 0.5 * torch.sum(Dn * (Hs[gi] + F), dim=(1, 2))
-                dE = (En - E[gi]).abs().max()
-                rmsd = torch.sqrt(torch.sum((Dn - be.view(self.D, g)) ** 2, dim=(1, 2))).max()
-                if not (float(dE) < dE_threshold and float(rmsd) < rmsd_threshold):
-                    conv_all = False
+                En = 0.5 * torch.sum(Dn * (Hs[gi] + Fx[gi]), dim=(1, 2))
+                stats[gi, 0] = (En - E[gi]).abs().max()
+                stats[gi, 1] = torch.sqrt(torch.sum((Dn - be.view(self.D, g)) ** 2, dim=(1, 2))).max()
+                if diis[gi].last_error is not None:  # None: DIIS is off for 2-function molecules
+                    stats[gi, 2] = diis[gi].last_error.max()
                 be.view(self.D, g).copy_(Dn)
                 newE.append(En)
             E = newE
-            if switch and mode == "mixed":
+            st = stats.cpu().numpy()  # the one host synchronisation of the iteration
+            conv_all = bool(np.all(st[:, 0] < dE_threshold) and np.all(st[:, 1] < rmsd_threshold))
+            if mode == "mixed" and bool(np.all(st[:, 2] < self.tail)):
                 mode = "fp64"
                 diis = [_BatchDIIS(len(g.mols), g.nbf, be.device) for g in be.groups]
                 conv_all = False

@@ -93,14 +93,18 @@ static int check_common(const char *who, const sq_basis *basis, const sq_pairs *
 // so they are spread over a small pool of streams forked from and joined back
 // into the caller's stream: the tail of one class overlaps the start of the
 // next.  g_jk_streams = 1 keeps every launch on the caller's stream.
-static int g_jk_streams = 4;
-constexpr int kMaxPoolStreams = 8;
+// Successive calls take the next streams of the pool (round robin), so two
+// calls issued from different caller streams (the FP64 and FP32 lists of a
+// mixed build) do not queue behind each other.
+static int g_jk_streams = 8;
+constexpr int kMaxPoolStreams = 16;
 constexpr int kMaxPoolDevices = 64;
 
 struct StreamPool {
     bool ready = false;
+    int next = 0;
     cudaStream_t s[kMaxPoolStreams];
-    cudaEvent_t fork;
+    cudaEvent_t fork[kMaxPoolStreams];
     cudaEvent_t join[kMaxPoolStreams];
 };
 static StreamPool g_pool[kMaxPoolDevices];
@@ -114,9 +118,10 @@ static int pool_for_current_device(StreamPool **out) {
     if (dev < 0 || dev >= kMaxPoolDevices) return set_error(SQ_ERR_ARG, "stream pool: device %d out of range", dev);
     StreamPool &p = g_pool[dev];
     if (!p.ready) {
-        e = cudaEventCreateWithFlags(&p.fork, cudaEventDisableTiming);
+        e = cudaSuccess;
         for (int i = 0; i < kMaxPoolStreams && e == cudaSuccess; ++i) {
             e = cudaStreamCreateWithFlags(&p.s[i], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p.fork[i], cudaEventDisableTiming);
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p.join[i], cudaEventDisableTiming);
         }
         if (e != cudaSuccess) return set_error(SQ_ERR_CUDA, "stream pool: %s", cudaGetErrorString(e));
@@ -158,12 +163,15 @@ static int run_classes(const char *who, EriArgs args, const sq_quartets *qs, int
         StreamPool *pool = nullptr;
         int rc = pool_for_current_device(&pool);
         if (rc) return rc;
-        cudaError_t e = cudaEventRecord(pool->fork, stream);
-        for (int i = 0; i < nstream && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(pool->s[i], pool->fork, 0);
+        const int first = pool->next;
+        pool->next = (pool->next + nstream) % kMaxPoolStreams;
+        auto sid = [&](int i) { return (first + i) % kMaxPoolStreams; };
+        cudaError_t e = cudaEventRecord(pool->fork[first], stream);
+        for (int i = 0; i < nstream && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(pool->s[sid(i)], pool->fork[first], 0);
         int k = 0;
         for (int c = 0; c < SQ_MAX_QCLASS && e == cudaSuccess; ++c) {
             if (qs->class_off[c + 1] == qs->class_off[c]) continue;
-            e = launch_class(args, qs, c, mode, precision, pool->s[k++ % nstream]);
+            e = launch_class(args, qs, c, mode, precision, pool->s[sid(k++ % nstream)]);
             if (e != cudaSuccess) {
                 set_error(SQ_ERR_CUDA, "%s: class %d: %s", who, c, cudaGetErrorString(e));
                 break;
@@ -171,8 +179,8 @@ static int run_classes(const char *who, EriArgs args, const sq_quartets *qs, int
         }
         // always join what was forked, so the caller's stream (or a capture) stays whole
         for (int i = 0; i < nstream; ++i) {
-            cudaError_t ej = cudaEventRecord(pool->join[i], pool->s[i]);
-            if (ej == cudaSuccess) ej = cudaStreamWaitEvent(stream, pool->join[i], 0);
+            cudaError_t ej = cudaEventRecord(pool->join[sid(i)], pool->s[sid(i)]);
+            if (ej == cudaSuccess) ej = cudaStreamWaitEvent(stream, pool->join[sid(i)], 0);
             if (e == cudaSuccess) e = ej;
         }
         if (e != cudaSuccess) return set_error(SQ_ERR_CUDA, "%s: %s", who, cudaGetErrorString(e));

@@ -37,15 +37,20 @@ from dataclasses import dataclass
 import numpy as np
 import torch
 
-from . import _lib, screening
+from . import _lib, flops, screening
 from ._lib import SqBasis, SqPairs, SqQuartets, SqSlots, check, ptr
 from .molecule import _Molecule
 
 NCART = [1, 3, 6, 10]
 # bound on |(ij|kl)| of a primitive quartet below which primitive pair ij is left out
 PRIM_SCREEN = 1e-17
-# primitive quartets per thread above which a J/K quartet is split over its bra primitives
+# work per thread, in (ss|ss) primitive quartets, above which a J/K quartet is
+# split over its bra primitives (a class's primitive quartet weighs its model
+# FLOPs over those of (ss|ss))
 SPLIT_TARGET = 512
+_W_SSSS = flops.flops_per_primitive_quartet(0, 0, 0, 0)
+CLASS_WEIGHT = [flops.flops_per_primitive_quartet(*flops.quartet_class_l(c)) / _W_SSSS
+                for c in range(screening.NQCLASS)]
 
 
 def herm_size(la: int, lb: int) -> int:
@@ -390,9 +395,12 @@ class IntegralEngine:
         la_s = self.l[self.pair_shells[slot_pair, 0]] if nslot else np.zeros(0, np.int32)
         lb_s = self.l[self.pair_shells[slot_pair, 1]] if nslot else np.zeros(0, np.int32)
         E_s = np.array([herm_size(int(a), int(b)) for a, b in zip(la_s, lb_s)], dtype=np.int64)
+        # heaviest quartet class a slot can be the bra of: (its pair class | its pair class)
+        pc_s = self.pair_class[slot_pair] if nslot else np.zeros(0, np.int64)
+        w_s = np.array([CLASS_WEIGHT[screening.quartet_class(int(c), int(c))] for c in pc_s], dtype=np.float64)
         S = 2
         while nslot:
-            want = (npp.astype(np.int64) * max_np > SPLIT_TARGET * (S // 2)) & (npp >= S)
+            want = (npp * max_np * w_s > SPLIT_TARGET * (S // 2)) & (npp >= S)
             idx = np.nonzero(want)[0]
             if len(idx) == 0:
                 break
@@ -492,7 +500,7 @@ class IntegralEngine:
             for m, st, n in tasks[c]:
                 slots = self.slot_of_pair[m]
                 if c <= split_max_class and len(m):
-                    cost = int(npp[slots[0]]) * int(npp[self.slot_of_pair[ket_list[st[0]]]])
+                    cost = int(npp[slots[0]]) * int(npp[self.slot_of_pair[ket_list[st[0]]]]) * CLASS_WEIGHT[c]
                     S = 1
                     while cost > SPLIT_TARGET * S and (2 * S) in self.sub_first and \
                             self.sub_first[2 * S][slots[0]] >= 0:
@@ -571,14 +579,29 @@ class IntegralEngine:
         Jacc.zero_()
         Kacc.zero_()
         D = D.contiguous()
-        for ql, prec in zip(lists, precisions):
-            if ql.nquartet == 0:
-                continue
+        work = [(ql, prec) for ql, prec in zip(lists, precisions) if ql.nquartet]
+        main = torch.cuda.current_stream(self.device)
+        # the lists after the first run from side streams, concurrently with the
+        # first (all of them only add into Jacc/Kacc)
+        side = self._side_streams(len(work) - 1)
+        for s in side:
+            s.wait_stream(main)  # after the zeroing, before the first list's launches
+        for i, (ql, prec) in enumerate(work):
+            s = main if i == 0 else side[i - 1]
             qs = ql.cstruct()
             check(self.lib.sq_jk(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(self.slots),
                                  ctypes.byref(qs), ptr(self.tab64), ptr(self.tab32), ptr(D), ptr(D32), ptr(Jacc),
-                                 ptr(Kacc), _lib.PRECISIONS[prec], self._stream()), "sq_jk")
+                                 ptr(Kacc), _lib.PRECISIONS[prec], s.cuda_stream), "sq_jk")
+        for s in side:
+            main.wait_stream(s)
         return Jacc, Kacc
+
+    def _side_streams(self, n: int):
+        if not hasattr(self, "_sides"):
+            self._sides = []
+        while len(self._sides) < n:
+            self._sides.append(torch.cuda.Stream(self.device))
+        return self._sides[:n]
 
     def jk_multi(self, Ds: torch.Tensor, threshold: float = 1e-12, precision: str = "fp64",
                  fp32_threshold: float = 1e-4):

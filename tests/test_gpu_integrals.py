@@ -247,7 +247,7 @@ def test_jk_stream_pool_matches_single_stream():
         J1, K1 = (x.cpu().numpy() for x in eng.jk(D, 1e-12, "mixed", 1e-4))
         _lib.check(L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, 8), "sq_set_option")
         J8, K8 = (x.cpu().numpy() for x in eng.jk(D, 1e-12, "mixed", 1e-4))
-        assert L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, 9) != 0  # out of range is rejected
+        assert L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, 17) != 0  # out of range is rejected
     finally:
         L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, default)
     np.testing.assert_allclose(J8, J1, atol=1e-11)
