@@ -385,6 +385,19 @@ def gpu_arm(args) -> None:
                       "dE_one_build": dE_build, "dE_scf": Et - E64,
                       "mixed_builds": sum(1 for b in jkt.builds if b != "fp64"), "builds": len(jkt.builds)})
 
+    # primitive-chunk granularity of the same precision test (beside the headline)
+    chunk_modes = []
+    for tau in (FP32_THR, 1e-3):
+        eng.fock(H, D, SCREEN, "mixed_chunk", tau)
+        ms_c = float(np.median(time_events(torch, lambda: eng.fock(H, D, SCREEN, "mixed_chunk", tau), 5, flush)))
+        Fc = eng.fock(H, D, SCREEN, "mixed_chunk", tau)
+        jkc = DirectJK(eng, SCREEN, "mixed_chunk", tau, 1e-5)
+        Ec, _, _, _ = run_hartree_fock(S, T, V, jkc, ne, log, 1e-9, 1e-9, 100, True)
+        c64, c32 = eng.quartets(SCREEN, tau, chunks=True)
+        chunk_modes.append({"fp32_threshold": tau, "fock_build_ms": ms_c, "speedup_vs_fp64": ms64 / ms_c,
+                            "dE_one_build": float(0.5 * torch.sum(D * (H + Fc))) - E_build64, "dE_scf": Ec - E64,
+                            "fp64_entries": c64.nquartet, "fp32_entries": c32.nquartet})
+
     # the two halves of the mixed build, each timed alone (all its classes, stream pool)
     ms_part = {}
     for name, lst, prec in (("fp64_list", q64, "fp64"), ("fp32_list", q32, "fp32")):
@@ -442,6 +455,7 @@ def gpu_arm(args) -> None:
         "roofline_fp64_build": {"flops": fl64, "ms": ms64, "achieved_tflops": fl64 / (ms64 * 1e-3) / 1e12,
                                 "peak_tflops": peak64 / 1e12, "frac": fl64 / (ms64 * 1e-3) / peak64},
         "tau_sweep": sweep,
+        "chunk_precision": chunk_modes,
         "kernels_by_time": rows[:8],
         "gpu_launches": launches * args.steps,
         "clocks": clocks,

@@ -44,6 +44,17 @@ struct WarpSmem {
     R Fs[16];
 };
 
+// J/K epilogue scratch (FP64), overlaid on a warp's shared memory after its
+// primitive loops: the integral block, then the six density blocks.  A warp's
+// slice is the larger of the two uses, rounded to 16 bytes.
+constexpr int kWarpBlk = ncart(SQ_LMAX) * ncart(SQ_LMAX);
+constexpr int kWarpEpi = kWarpBlk * kWarpBlk + 6 * kWarpBlk;
+template <typename R>
+__host__ __device__ constexpr size_t warp_stride() {
+    return ((sizeof(WarpSmem<R>) > kWarpEpi * sizeof(double) ? sizeof(WarpSmem<R>) : kWarpEpi * sizeof(double)) +
+            15) / 16 * 16;
+}
+
 __device__ __forceinline__ void cart_powers(int l, int c, int &x, int &y, int &z) {
     int idx = 0;
     for (int xx = l; xx >= 0; --xx)
@@ -79,7 +90,7 @@ template <typename R, int BOYS, int MODE>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const EriArgs args, const WarpClass cls) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    WarpSmem<R> &sm = reinterpret_cast<WarpSmem<R> *>(smem_raw)[warp];
+    WarpSmem<R> &sm = *reinterpret_cast<WarpSmem<R> *>(smem_raw + warp * warp_stride<R>());
     // per-block tables: (t,u,v) of each flat Hermite index; E offsets of component pairs
     __shared__ int s_tuv[kWarpHmax];
     __shared__ short s_hoff_b[ncart(SQ_LMAX) * ncart(SQ_LMAX)];
@@ -304,11 +315,94 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
             if (lane == 0) args.q[P] = sqrt(mx);
-        } else {
+        } else if constexpr (MODE == MODE_JK) {
+            // J/K digestion in two steps, like the per-thread kernel: the warp
+            // stages the integral block and the six density blocks in shared
+            // memory, contracts them to the J and K blocks, and issues one atomic
+            // per J/K block element (NAB + NCD + 4 mixed blocks) instead of six
+            // per integral.
             double m = 8.0;
             if (sa == sb) m *= 0.5;
             if (sc == sd) m *= 0.5;
             if (P == Q) m *= 0.5;
+            const double wJ = 0.5 * m, wK = 0.25 * m;
+            const sq_basis &bs = args.basis;
+            double *ep = reinterpret_cast<double *>(&sm);
+            double *Vb = ep;                          // [NAB][NCD]
+            double *Dab = ep + kWarpBlk * kWarpBlk;   // [NA][NB]
+            double *Dcd = Dab + kWarpBlk;             // [NC][ND]
+            double *Dac = Dcd + kWarpBlk;             // [NA][NC]
+            double *Dbd = Dac + kWarpBlk;             // [NB][ND]
+            double *Dad = Dbd + kWarpBlk;             // [NA][ND]
+            double *Dbc = Dad + kWarpBlk;             // [NB][NC]
+            __syncwarp();
+#pragma unroll
+            for (int kk = 0; kk < kWarpAccMax; ++kk)
+                if (kk < kacc && lane + 32 * kk < NACC) Vb[lane + 32 * kk] = (double)acc[kk];
+            const int nd = args.nd > 1 ? args.nd : 1;
+            const int nJ = NAB + NCD, nK = NA * NC + NB * ND + NA * ND + NB * NC;
+            for (int di = 0; di < nd; ++di) {
+                const double *D = args.D + di * args.dstride;
+                double *J = args.Jacc + di * args.dstride, *K = args.Kacc + di * args.dstride;
+                for (int x = lane; x < NAB; x += 32) Dab[x] = gload(D + mat_index(bs, sa, x / NB, sb, x % NB));
+                for (int x = lane; x < NCD; x += 32) Dcd[x] = gload(D + mat_index(bs, sc, x / ND, sd, x % ND));
+                for (int x = lane; x < NA * NC; x += 32) Dac[x] = gload(D + mat_index(bs, sa, x / NC, sc, x % NC));
+                for (int x = lane; x < NB * ND; x += 32) Dbd[x] = gload(D + mat_index(bs, sb, x / ND, sd, x % ND));
+                for (int x = lane; x < NA * ND; x += 32) Dad[x] = gload(D + mat_index(bs, sa, x / ND, sd, x % ND));
+                for (int x = lane; x < NB * NC; x += 32) Dbc[x] = gload(D + mat_index(bs, sb, x / NC, sc, x % NC));
+                __syncwarp();
+                for (int o = lane; o < nJ + nK; o += 32) {
+                    double sum = 0.0;
+                    long long dst;
+                    double *T;
+                    double w;
+                    if (o < NAB) {  // J_ab = sum_cd (ab|cd) D_cd
+                        for (int cd = 0; cd < NCD; ++cd) sum = fma(Vb[o * NCD + cd], Dcd[cd], sum);
+                        dst = mat_index(bs, sa, o / NB, sb, o % NB);
+                        T = J;
+                        w = wJ;
+                    } else if (o < nJ) {  // J_cd = sum_ab (ab|cd) D_ab
+                        const int cd = o - NAB;
+                        for (int ab = 0; ab < NAB; ++ab) sum = fma(Vb[ab * NCD + cd], Dab[ab], sum);
+                        dst = mat_index(bs, sc, cd / ND, sd, cd % ND);
+                        T = J;
+                        w = wJ;
+                    } else {
+                        int r = o - nJ;
+                        T = K;
+                        w = wK;
+                        if (r < NA * NC) {  // K_ac = sum_bd (ab|cd) D_bd
+                            const int a = r / NC, c = r % NC;
+                            for (int b = 0; b < NB; ++b)
+                                for (int d = 0; d < ND; ++d)
+                                    sum = fma(Vb[(a * NB + b) * NCD + c * ND + d], Dbd[b * ND + d], sum);
+                            dst = mat_index(bs, sa, a, sc, c);
+                        } else if ((r -= NA * NC) < NB * ND) {  // K_bd = sum_ac (ab|cd) D_ac
+                            const int b = r / ND, d = r % ND;
+                            for (int a = 0; a < NA; ++a)
+                                for (int c = 0; c < NC; ++c)
+                                    sum = fma(Vb[(a * NB + b) * NCD + c * ND + d], Dac[a * NC + c], sum);
+                            dst = mat_index(bs, sb, b, sd, d);
+                        } else if ((r -= NB * ND) < NA * ND) {  // K_ad = sum_bc (ab|cd) D_bc
+                            const int a = r / ND, d = r % ND;
+                            for (int b = 0; b < NB; ++b)
+                                for (int c = 0; c < NC; ++c)
+                                    sum = fma(Vb[(a * NB + b) * NCD + c * ND + d], Dbc[b * NC + c], sum);
+                            dst = mat_index(bs, sa, a, sd, d);
+                        } else {  // K_bc = sum_ad (ab|cd) D_ad
+                            r -= NA * ND;
+                            const int b = r / NC, c = r % NC;
+                            for (int a = 0; a < NA; ++a)
+                                for (int d = 0; d < ND; ++d)
+                                    sum = fma(Vb[(a * NB + b) * NCD + c * ND + d], Dad[a * ND + d], sum);
+                            dst = mat_index(bs, sb, b, sc, c);
+                        }
+                    }
+                    atomicAdd(T + dst, w * sum);
+                }
+                __syncwarp();  // the density blocks are reloaded for the next density / quartet
+            }
+        } else {
 #pragma unroll
             for (int kk = 0; kk < kWarpAccMax; ++kk) {
                 if (kk < kacc) {
@@ -327,24 +421,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
                             V[((Dd * n + C) * n + A) * n + B] = v;
                             V[((C * n + Dd) * n + B) * n + A] = v;
                             V[((Dd * n + C) * n + B) * n + A] = v;
-                        } else {
-                            const double wJ = 0.5 * m * v, wK = 0.25 * m * v;
-                            const sq_basis &bs = args.basis;
-                            const int a = ab / NB, b = ab % NB, c = cd / ND, d = cd % ND;
-                            const long long iab = mat_index(bs, sa, a, sb, b), icd = mat_index(bs, sc, c, sd, d);
-                            const long long iac = mat_index(bs, sa, a, sc, c), ibd = mat_index(bs, sb, b, sd, d);
-                            const long long iad = mat_index(bs, sa, a, sd, d), ibc = mat_index(bs, sb, b, sc, c);
-                            const int nd = args.nd > 1 ? args.nd : 1;
-                            for (int di = 0; di < nd; ++di) {
-                                const double *D = args.D + di * args.dstride;
-                                double *J = args.Jacc + di * args.dstride, *K = args.Kacc + di * args.dstride;
-                                atomicAdd(J + iab, wJ * gload(D + icd));
-                                atomicAdd(J + icd, wJ * gload(D + iab));
-                                atomicAdd(K + iac, wK * gload(D + ibd));
-                                atomicAdd(K + ibd, wK * gload(D + iac));
-                                atomicAdd(K + iad, wK * gload(D + ibc));
-                                atomicAdd(K + ibc, wK * gload(D + iad));
-                            }
                         }
                     }
                 }
@@ -355,7 +431,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
 
 template <typename R>
 constexpr size_t warp_smem_bytes() {
-    return sizeof(WarpSmem<R>) * kWarpsPerBlock;
+    return warp_stride<R>() * kWarpsPerBlock;
 }
 
 inline cudaError_t launch_eri_warp(const EriArgs &args, const WarpClass &cls, int mode, int precision,

@@ -380,9 +380,18 @@ class IntegralEngine:
         first = np.repeat(np.concatenate([[0], np.cumsum(lens)[:-1]]), lens)
         gidx = np.repeat(starts, lens) + (np.arange(int(lens.sum())) - first)
         kept = self._keep[gidx]
-        prim_src = (gidx - np.repeat(starts, lens))[kept].astype(np.int32)
+        # each slot's kept primitive pairs in descending primitive Schwarz factor,
+        # so that chunk 0 of a sub-slot split holds the largest ones
+        slot_of_entry = np.repeat(np.arange(nslot), lens)[kept]
+        gk = gidx[kept]
+        order = np.lexsort((-self.prim_q[gk], slot_of_entry))
+        gk = gk[order]
+        prim_src = (gk - np.repeat(starts, npp)).astype(np.int32)
         prim_src_off = np.concatenate([[0], np.cumsum(npp)[:-1]]).astype(np.int64)
         assert len(prim_src) == int(npp.sum())
+        # prefix sums of the sorted factors: the bound sum_ij q_ij of any chunk
+        qsorted = self.prim_q[gk]
+        qcum = np.concatenate([[0.0], np.cumsum(qsorted)])
         self.slot_of_pair = np.empty(nslot, np.int32)
         self.slot_of_pair[slot_pair] = np.arange(nslot, dtype=np.int32)
         # sub-slots: S (a power of two) chunks of a slot's primitive pairs, for the
@@ -390,7 +399,7 @@ class IntegralEngine:
         # primitive pairs [k*n//S, (k+1)*n//S) of its parent and shares its data
         max_np = int(npp.max()) if nslot else 0
         self.sub_first: dict[int, np.ndarray] = {}
-        sub_pair, sub_npp, sub_pb, sub_ps, sub_hb, sub_code = [], [], [], [], [], []
+        sub_pair, sub_npp, sub_pb, sub_ps, sub_hb, sub_code, sub_qsum = [], [], [], [], [], [], []
         nsub = 0
         la_s = self.l[self.pair_shells[slot_pair, 0]] if nslot else np.zeros(0, np.int32)
         lb_s = self.l[self.pair_shells[slot_pair, 1]] if nslot else np.zeros(0, np.int32)
@@ -400,7 +409,7 @@ class IntegralEngine:
         w_s = np.array([CLASS_WEIGHT[screening.quartet_class(int(c), int(c))] for c in pc_s], dtype=np.float64)
         S = 2
         while nslot:
-            want = (npp * max_np * w_s > SPLIT_TARGET * (S // 2)) & (npp >= S)
+            want = ((npp * max_np * w_s > SPLIT_TARGET * (S // 2)) | (npp >= 4 * S)) & (npp >= S)
             idx = np.nonzero(want)[0]
             if len(idx) == 0:
                 break
@@ -417,6 +426,7 @@ class IntegralEngine:
             sub_ps.append(pstride[par])
             sub_hb.append(hbase[par] + lo * E_s[par] * pstride[par])
             sub_code.append((k << 16) | S)
+            sub_qsum.append(qcum[prim_src_off[par] + hi] - qcum[prim_src_off[par] + lo])
             nsub += S * len(idx)
             S *= 2
         self.nslot_base = nslot
@@ -428,6 +438,11 @@ class IntegralEngine:
             hbase = np.concatenate([hbase] + sub_hb).astype(np.int64)
         sub = np.concatenate([np.zeros(self.nslot_base, np.int64)] + sub_code).astype(np.int32)
         self.slot_sub = sub
+        # sum of the primitive Schwarz factors of every slot and sub-slot: a bound on
+        # its partial contracted factor, |(chunk|ket)| <= qsum[chunk] * qsum[ket]
+        base_qsum = qcum[prim_src_off + npp[: self.nslot_base]] - qcum[prim_src_off] if self.nslot_base else \
+            np.zeros(0)
+        self.slot_qsum = np.concatenate([base_qsum] + sub_qsum) if nsub else base_qsum
         self.slot_pair = slot_pair
         self.slot_npp = npp
         nslot = len(slot_pair)
@@ -466,14 +481,18 @@ class IntegralEngine:
 
     # -------------------------------------------------------------- quartets
     def quartets(self, threshold: float, fp32_threshold: float | None = None, q: np.ndarray | None = None,
-                 split: bool = True):
+                 split: bool = True, chunks: bool = False):
         """Unique screened quartets.  Returns one QuartetList, or (fp64, fp32) lists
         when fp32_threshold is given (bound >= fp32_threshold goes to FP64).
         ``q`` overrides the per-pair Schwarz factors (None: the engine's own).
         ``split``: heavy quartets of the per-thread J/K classes are emitted as
         bra sub-slot chunks (J/K lists only; dense tensors and gradients need
-        whole quartets)."""
-        key = (float(threshold), None if fp32_threshold is None else float(fp32_threshold), bool(split))
+        whole quartets).  ``chunks`` (with fp32_threshold): the precision test
+        is applied per bra chunk of the FP64 quartets of the per-thread classes:
+        a chunk goes to FP32 when the sum of its primitive Schwarz factors times
+        the ket's is below fp32_threshold."""
+        key = (float(threshold), None if fp32_threshold is None else float(fp32_threshold), bool(split),
+               bool(chunks))
         if q is None and key in self._quartet_cache:
             return self._quartet_cache[key]
         self._require_eri()
@@ -485,11 +504,73 @@ class IntegralEngine:
         self.slots  # canonical slot numbering (from the engine's own Schwarz factors)
         # classes with per-thread kernels: 0-11 in FP64, 0-18 in FP32
         split_max = [11, 18] if split else [-1, -1]
-        out = [self._expand(t, ket_list, split_max[li]) for li, t in enumerate(lists)]
+        if chunks and fp32_threshold is not None:
+            out = self._chunk_lists(lists, ket_list, float(fp32_threshold))
+        else:
+            out = [self._expand(t, ket_list, split_max[li]) for li, t in enumerate(lists)]
         res = out[0] if len(out) == 1 else (out[0], out[1])
         if own:
             self._quartet_cache[key] = res
         return res
+
+    def _chunk_lists(self, lists, ket_list: np.ndarray, tau: float):
+        """(FP64, FP32) lists with the precision test per bra primitive chunk.
+
+        FP64 quartets of the per-thread classes (0-11) are cut into S chunks of
+        their bra's primitive pairs (sorted by descending factor, about 4-8 per
+        chunk, more when the quartet is heavy), and each chunk is placed by its
+        own bound qsum[chunk] * qsum[ket]; FP32 quartets stay whole.
+        """
+        t64, t32 = lists
+        q32 = self._expand(t32, ket_list, 18)
+        npp = self.slot_npp
+        ket_slots = self.slot_of_pair[ket_list]
+        keep64 = {c: [] for c in range(screening.NQCLASS)}
+        move32 = {c: [] for c in range(screening.NQCLASS)}
+        whole64 = {c: [] for c in range(screening.NQCLASS)}
+        for c in range(screening.NQCLASS):
+            for m, st, n in t64[c]:
+                slots = self.slot_of_pair[m]
+                if c > 11 or len(m) == 0:
+                    whole64[c].append((m, st, n))  # pair ids: _expand maps them to slots
+                    continue
+                nb = int(npp[slots[0]])
+                cost = nb * int(npp[ket_slots[st[0]]]) * CLASS_WEIGHT[c]
+                S = 1
+                while (2 * S) in self.sub_first and self.sub_first[2 * S][slots[0]] >= 0 and \
+                        (nb >= 8 * S or cost > SPLIT_TARGET * S):
+                    S *= 2
+                pairs = screening.expand_host(slots.astype(np.int32), st.astype(np.int32), n.astype(np.int64),
+                                              ket_slots)
+                if S == 1:
+                    chunk = pairs
+                else:
+                    first = self.sub_first[S][pairs[:, 0]]
+                    chunk = np.concatenate([np.stack([(first + k).astype(np.int32), pairs[:, 1]], 1)
+                                            for k in range(S)])
+                big = self.slot_qsum[chunk[:, 0]] * self.slot_qsum[chunk[:, 1]] >= tau
+                keep64[c].append(chunk[big])
+                move32[c].append(chunk[~big])
+        # FP64 list: whole-quartet blocks of the warp classes (device expand) and
+        # the kept chunks; FP32 list: the quartet-level FP32 list plus the moved chunks
+        q64w = self._expand(whole64, ket_list, -1)
+        dev = self.device
+
+        def merge(base, extra):
+            parts, off = [], np.zeros(screening.NQCLASS + 1, dtype=np.int64)
+            for c in range(screening.NQCLASS):
+                seg = base.pairs[base.class_off[c]:base.class_off[c + 1]] if base is not None else None
+                ex = np.concatenate(extra[c]) if extra[c] else np.zeros((0, 2), np.int32)
+                n = (0 if seg is None else int(base.class_off[c + 1] - base.class_off[c])) + len(ex)
+                off[c + 1] = off[c] + n
+                if seg is not None and len(seg):
+                    parts.append(seg[: int(base.class_off[c + 1] - base.class_off[c])])
+                if len(ex):
+                    parts.append(torch.tensor(ex.astype(np.int32), device=dev))
+            pairs = torch.cat(parts).contiguous() if parts else torch.empty((1, 2), dtype=torch.int32, device=dev)
+            return QuartetList(pairs, off)
+
+        return [merge(q64w, keep64), merge(q32, move32)]
 
     def _split_tasks(self, tasks: dict, ket_list: np.ndarray, split_max_class: int) -> dict:
         """Bra slot ids of every task block, heavy blocks replaced by their sub-slot chunks."""
@@ -603,16 +684,26 @@ class IntegralEngine:
             self._sides.append(torch.cuda.Stream(self.device))
         return self._sides[:n]
 
+    def _lists_for(self, precision: str, threshold: float, fp32_threshold: float):
+        """Quartet lists and their launch precisions for a J/K precision mode.
+
+        "fp64": every quartet FP64; "mixed": quartets with bound < fp32_threshold
+        in FP32 (FP64 Boys recursion); "mixed_boys32": the same, recursion in FP32
+        too; "mixed_chunk": the "mixed" test applied per bra primitive chunk of
+        the large-bound quartets (classes with per-thread kernels).
+        """
+        if precision == "fp64":
+            return [self.quartets(threshold)], ["fp64"]
+        if precision not in ("mixed", "mixed_boys32", "mixed_chunk"):
+            raise ValueError(f"unknown precision {precision!r}")
+        q64, q32 = self.quartets(threshold, fp32_threshold, chunks=precision == "mixed_chunk")
+        return [q64, q32], ["fp64", "fp32_boys32" if precision == "mixed_boys32" else "fp32"]
+
     def jk_multi(self, Ds: torch.Tensor, threshold: float = 1e-12, precision: str = "fp64",
                  fp32_threshold: float = 1e-4):
         """J_i, K_i (symmetrised, [nd, nbf, nbf]) for a stack of densities Ds [nd, nbf, nbf],
         with each quartet's integrals evaluated once for all of them (sq_jk_multi)."""
-        if precision == "fp64":
-            lists, precs = [self.quartets(threshold)], ["fp64"]
-        else:
-            q64, q32 = self.quartets(threshold, fp32_threshold)
-            lists = [q64, q32]
-            precs = ["fp64", "fp32" if precision == "mixed" else "fp32_boys32"]
+        lists, precs = self._lists_for(precision, threshold, fp32_threshold)
         Ds = Ds.to(device=self.device, dtype=torch.float64).contiguous()
         nd = Ds.shape[0]
         Jacc = torch.zeros_like(Ds)
@@ -636,12 +727,7 @@ class IntegralEngine:
         precision: "fp64" (every quartet FP64), "mixed" (bound < fp32_threshold
         in FP32 with FP64 Boys), "mixed_boys32" (those quartets fully FP32).
         """
-        if precision == "fp64":
-            lists, precs = [self.quartets(threshold)], ["fp64"]
-        else:
-            q64, q32 = self.quartets(threshold, fp32_threshold)
-            lists = [q64, q32]
-            precs = ["fp64", "fp32" if precision == "mixed" else "fp32_boys32"]
+        lists, precs = self._lists_for(precision, threshold, fp32_threshold)
         Jacc, Kacc = self.jk_accumulate(D, lists, precs)
         J = torch.empty_like(Jacc)
         K = torch.empty_like(Kacc)
@@ -652,12 +738,7 @@ class IntegralEngine:
     def fock(self, H: torch.Tensor, D: torch.Tensor, threshold: float = 1e-12, precision: str = "fp64",
              fp32_threshold: float = 1e-4) -> torch.Tensor:
         """F = H + J - K/2 built directly from screened ERIs."""
-        if precision == "fp64":
-            lists, precs = [self.quartets(threshold)], ["fp64"]
-        else:
-            q64, q32 = self.quartets(threshold, fp32_threshold)
-            lists = [q64, q32]
-            precs = ["fp64", "fp32" if precision == "mixed" else "fp32_boys32"]
+        lists, precs = self._lists_for(precision, threshold, fp32_threshold)
         Jacc, Kacc = self.jk_accumulate(D, lists, precs)
         F = torch.empty_like(Jacc)
         check(self.lib.sq_fock_build(self.nbf, ptr(H.contiguous()), ptr(Jacc), ptr(Kacc), ptr(F), None, None,

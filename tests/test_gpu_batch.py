@@ -71,14 +71,15 @@ def test_batch_mixed_precision(gpu_lib):
     assert np.max(np.abs(Em - E64)) < 1e-6
 
 
-def test_batched_eigh_ragged_matches_numpy(gpu_lib):
-    """sq_batched_eigh on matrices of mixed sizes (1..128) against numpy eigh."""
+@pytest.mark.parametrize("dims", [[1, 2, 7, 19, 38, 57, 114, 128],  # eigenvectors rotated in global memory
+                                  [3, 18, 55, 76, 95, 114, 118]])     # eigenvectors in shared memory
+def test_batched_eigh_ragged_matches_numpy(gpu_lib, dims):
+    """sq_batched_eigh on matrices of mixed sizes against numpy eigh."""
     import torch
 
     from slowquant_gb300 import _lib
 
     rng = np.random.default_rng(3)
-    dims = [1, 2, 7, 19, 38, 57, 114, 128]
     offs = np.concatenate([[0], np.cumsum([d * d for d in dims])[:-1]]).astype(np.int64)
     woff = np.concatenate([[0], np.cumsum(dims)[:-1]]).astype(np.int64)
     mats = []

@@ -252,3 +252,32 @@ def test_jk_stream_pool_matches_single_stream():
         L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, default)
     np.testing.assert_allclose(J8, J1, atol=1e-11)
     np.testing.assert_allclose(K8, K1, atol=1e-11)
+
+
+def test_chunk_level_mixed_precision():
+    """mixed_chunk: FP64 quartets' small primitive chunks in FP32; J/K at the FP32 error scale."""
+    import torch
+
+    from slowquant_gb300 import systems
+
+    eng = _engine(systems.water_cluster(3, 6.0, seed=3), "cc-pvdz", "angstrom")
+    D = torch.tensor(_random_density(eng.nbf, 6), dtype=torch.float64, device="cuda")
+    J0, K0 = (x.cpu().numpy() for x in eng.jk(D, 1e-12, "fp64"))
+    Jm, Km = (x.cpu().numpy() for x in eng.jk(D, 1e-12, "mixed", 1e-4))
+    Jc, Kc = (x.cpu().numpy() for x in eng.jk(D, 1e-12, "mixed_chunk", 1e-4))
+    assert np.max(np.abs(Jc - J0)) < 1e-6 and np.max(np.abs(Kc - K0)) < 1e-6
+    # the chunk lists keep fewer primitive quartets in FP64 than the quartet-level lists
+    npp = eng.slot_npp.astype(np.int64)
+
+    def prims(ql):
+        p = ql.pairs[: ql.nquartet].cpu().numpy()
+        return int((npp[p[:, 0]] * npp[p[:, 1]]).sum())
+
+    q64, q32 = eng.quartets(1e-12, 1e-4)
+    c64, c32 = eng.quartets(1e-12, 1e-4, chunks=True)
+    assert prims(c64) < prims(q64)
+    assert prims(c64) + prims(c32) == prims(q64) + prims(q32)  # same primitive quartets, re-partitioned
+    # every chunk kept in FP64 (per-thread classes 0-11) has a large bound
+    p = c64.pairs[: int(c64.class_off[12])].cpu().numpy()
+    assert np.all(eng.slot_qsum[p[:, 0]] * eng.slot_qsum[p[:, 1]] >= 1e-4)
+    assert np.max(np.abs(Jm - J0)) < 1e-6
