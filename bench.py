@@ -185,6 +185,18 @@ def time_events(torch, fn, n: int, flush=None) -> list[float]:
     return ts
 
 
+def max_over_ranks(value: float, world: int, device: str = "cpu") -> float:
+    """The largest of every rank's value (the slowest replica sets the timed region)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ----------------------------------------------------------------- CPU arm
 def cpu_sample(eng_or_none, target_seconds: float, seed: int = 0, pairs_host=None, mol_geom=None):
     """Time the oracle (faithful restatement of the reference) on random surviving quartets."""
@@ -344,10 +356,7 @@ def gpu_arm(args) -> None:
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     tot_mixed = sum(ms_mixed)
-    if world > 1:
-        t = torch.tensor([tot_mixed], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_mixed = float(t.item())
+    tot_mixed = max_over_ranks(tot_mixed, world, "cuda")
 
     ms_step = tot_mixed / args.steps
     nq = nq_unique

@@ -25,7 +25,7 @@ import torch
 
 from . import _lib, screening
 from ._lib import SqBasis, SqPairs, SqQuartets, SqSlots, check, ptr
-from .engine import QuartetList, herm_size
+from .engine import CLASS_WEIGHT, SPLIT_TARGET, QuartetList, herm_size
 from .molecule import _Molecule
 
 
@@ -216,9 +216,27 @@ class BatchEngine:
             pos += n
             poff += n * nppg
             hoff += n * nppg * E
-        self.slot_pair = slot_pair
         self.slot_of_pair = np.empty(nslot, np.int32)
         self.slot_of_pair[slot_pair] = np.arange(nslot, dtype=np.int32)
+        # bra sub-slots for splitting heavy quartets (as in IntegralEngine)
+        la_s = self.l[self.pair_shells[slot_pair, 0]]
+        lb_s = self.l[self.pair_shells[slot_pair, 1]]
+        E_s = np.array([herm_size(int(a), int(b)) for a, b in zip(la_s, lb_s)], dtype=np.int64)
+        pc_s = self.pair_class[slot_pair]
+        w_s = np.array([CLASS_WEIGHT[screening.quartet_class(int(c), int(c))] for c in pc_s], dtype=np.float64)
+        qzero = np.zeros(int(npp.sum()) + 1)
+        off = np.concatenate([[0], np.cumsum(npp)[:-1]]).astype(np.int64)
+        self.sub_first, subs = screening.sub_slot_table(npp, pbase, pstride, hbase, E_s, w_s, qzero, off,
+                                                        int(npp.max()), SPLIT_TARGET)
+        self.nslot_base = nslot
+        slot_pair = np.concatenate([slot_pair, slot_pair[subs["parent"]]]).astype(np.int32)
+        npp = np.concatenate([npp, subs["npp"]]).astype(np.int32)
+        pbase = np.concatenate([pbase, subs["pbase"]]).astype(np.int32)
+        pstride = np.concatenate([pstride, subs["pstride"]]).astype(np.int32)
+        hbase = np.concatenate([hbase, subs["hbase"]]).astype(np.int64)
+        sub = np.concatenate([np.zeros(nslot, np.int64), subs["code"]]).astype(np.int32)
+        self.slot_pair = slot_pair
+        self.slot_npp = npp
         dev = self.device
         i32 = dict(dtype=torch.int32, device=dev)
         self.t_slot = [
@@ -227,14 +245,18 @@ class BatchEngine:
             torch.empty(5 * poff, dtype=torch.float64, device=dev), torch.empty(max(hoff, 1), dtype=torch.float64, device=dev),
             torch.empty(5 * poff, dtype=torch.float32, device=dev) if self.fp32 else None,
             torch.empty(max(hoff, 1), dtype=torch.float32, device=dev) if self.fp32 else None,
+            torch.tensor(sub, **i32),
         ]
         t = self.t_slot
         s = SqSlots()
-        s.nslot, s.npp_total, s.nherm_total = nslot, poff, hoff
+        s.nslot, s.npp_total, s.nherm_total = len(slot_pair), poff, hoff
         s.pair, s.npp, s.pbase, s.pstride, s.hbase = ptr(t[0]), ptr(t[1]), ptr(t[2]), ptr(t[3]), ptr(t[4])
         s.prim, s.herm, s.prim32, s.herm32 = ptr(t[5]), ptr(t[6]), ptr(t[7]), ptr(t[8])
+        s.sub = ptr(t[9])
         self.slots = s
-        check(self.lib.sq_slots_fill(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(s),
+        fill = SqSlots.from_buffer_copy(s)
+        fill.nslot = nslot  # the parents' data only: sub-slots point into it
+        check(self.lib.sq_slots_fill(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(fill),
                                      self._stream()), "sq_slots_fill")
 
     # ---------------------------------------------------------- quartets
@@ -257,7 +279,19 @@ class BatchEngine:
                 for c in range(screening.NQCLASS):
                     for bra, kst, cnt in lists[li][c]:
                         cost = int(self.pair_np[sel[bra[0]]] * self.pair_np[sel[ket[kst[0]]]])
-                        merged[li][c].append((cost, self.slot_of_pair[sel[bra]], ket_slots[kst], cnt))
+                        bslots = self.slot_of_pair[sel[bra]]
+                        # heavy quartets of the per-thread classes: bra sub-slot chunks
+                        S = 1
+                        if c <= (11 if li == 0 else 18):
+                            while cost * CLASS_WEIGHT[c] > SPLIT_TARGET * S and (2 * S) in self.sub_first and \
+                                    self.sub_first[2 * S][bslots[0]] >= 0:
+                                S *= 2
+                        if S == 1:
+                            merged[li][c].append((cost, bslots, ket_slots[kst], cnt))
+                        else:
+                            first = self.sub_first[S][bslots]
+                            for k in range(S):
+                                merged[li][c].append((cost / S, (first + k).astype(np.int32), ket_slots[kst], cnt))
         out = []
         for li in range(nl):
             tasks = {c: [(b, k, n) for _, b, k, n in sorted(merged[li][c], key=lambda t: -t[0])]

@@ -168,6 +168,10 @@ static int run_classes(const char *who, EriArgs args, const sq_quartets *qs, int
         auto sid = [&](int i) { return (first + i) % kMaxPoolStreams; };
         cudaError_t e = cudaEventRecord(pool->fork[first], stream);
         for (int i = 0; i < nstream && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(pool->s[sid(i)], pool->fork[first], 0);
+        // classes in index order (light, many-quartet classes first, the few
+        // high-L classes last), round robin over the streams; ordering by an
+        // estimate of each launch's work queued the heavy classes behind the
+        // long-running high-L ones on the same streams and measured slower
         int k = 0;
         for (int c = 0; c < SQ_MAX_QCLASS && e == cudaSuccess; ++c) {
             if (qs->class_off[c + 1] == qs->class_off[c]) continue;

@@ -86,7 +86,9 @@ __device__ __forceinline__ int herm_offset_rt(int la, int lb, int a, int b) {
     return off;
 }
 
-template <typename R, int BOYS, int MODE>
+// KACC: accumulator registers per lane (outputs / 32, rounded up to a bucket),
+// so that the smaller classes do not carry the (dd|dd) register footprint.
+template <typename R, int BOYS, int MODE, int KACC = kWarpAccMax>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const EriArgs args, const WarpClass cls) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -161,9 +163,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
         }
         const R *hb = herm + gload(pr.herm_off + P);
         const R *hk = herm + gload(pr.herm_off + Q);
-        R acc[kWarpAccMax];
+        R acc[KACC];
 #pragma unroll
-        for (int k = 0; k < kWarpAccMax; ++k) acc[k] = R(0);
+        for (int k = 0; k < KACC; ++k) acc[k] = R(0);
 
         for (int i = ib0; i < ib1; ++i) {
             const R p = gload(prim + 8 * i + 0);
@@ -281,7 +283,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
             // bra transform: lanes own output entries x = lane + 32 kk, x = ab * NCD + cd
             const R *eb = hb + (long long)(i - i0) * EB;
 #pragma unroll
-            for (int kk = 0; kk < kWarpAccMax; ++kk) {
+            for (int kk = 0; kk < KACC; ++kk) {
                 if (kk < kacc) {
                     const int x = lane + 32 * kk;
                     if (x < NACC) {
@@ -310,7 +312,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
         if constexpr (MODE == MODE_SCHWARZ) {
             double mx = -1e300;
 #pragma unroll
-            for (int kk = 0; kk < kWarpAccMax; ++kk)
+            for (int kk = 0; kk < KACC; ++kk)
                 if (kk < kacc && lane + 32 * kk < NACC) mx = fmax(mx, (double)acc[kk]);
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
@@ -337,7 +339,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
             double *Dbc = Dad + kWarpBlk;             // [NB][NC]
             __syncwarp();
 #pragma unroll
-            for (int kk = 0; kk < kWarpAccMax; ++kk)
+            for (int kk = 0; kk < KACC; ++kk)
                 if (kk < kacc && lane + 32 * kk < NACC) Vb[lane + 32 * kk] = (double)acc[kk];
             const int nd = args.nd > 1 ? args.nd : 1;
             const int nJ = NAB + NCD, nK = NA * NC + NB * ND + NA * ND + NB * NC;
@@ -404,7 +406,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
             }
         } else {
 #pragma unroll
-            for (int kk = 0; kk < kWarpAccMax; ++kk) {
+            for (int kk = 0; kk < KACC; ++kk) {
                 if (kk < kacc) {
                     const int x = lane + 32 * kk;
                     if (x < NACC) {
@@ -441,25 +443,34 @@ inline cudaError_t launch_eri_warp(const EriArgs &args, const WarpClass &cls, in
     const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : 152LL * 64;
     if (blocks > cap) blocks = cap;
     const dim3 grid((unsigned)blocks), block(32 * kWarpsPerBlock);
-#define SQ_WARP_LAUNCH(R, B, M)                                                                                 \
+#define SQ_WARP_LAUNCH(R, B, M, K)                                                                              \
     do {                                                                                                        \
-        auto kern = eri_warp_kernel<R, B, M>;                                                                   \
+        auto kern = eri_warp_kernel<R, B, M, K>;                                                                \
         const size_t sz = warp_smem_bytes<R>();                                                                 \
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sz);       \
         if (e != cudaSuccess) return e;                                                                         \
         kern<<<grid, block, sz, stream>>>(args, cls);                                                           \
     } while (0)
     // Dense tensors and Schwarz factors are drop-in outputs: reference-compatible Boys.
+    const int kacc = (ncart(cls.la) * ncart(cls.lb) * ncart(cls.lc) * ncart(cls.ld) + 31) / 32;
     if (mode == MODE_DENSE)
-        SQ_WARP_LAUNCH(double, BOYS_REF, MODE_DENSE);
+        SQ_WARP_LAUNCH(double, BOYS_REF, MODE_DENSE, kWarpAccMax);
     else if (mode == MODE_SCHWARZ)
-        SQ_WARP_LAUNCH(double, BOYS_REF, MODE_SCHWARZ);
-    else if (precision == SQ_FP64)
-        SQ_WARP_LAUNCH(double, BOYS_FP64, MODE_JK);
-    else if (precision == SQ_FP32)
-        SQ_WARP_LAUNCH(float, BOYS_FP64, MODE_JK);
+        SQ_WARP_LAUNCH(double, BOYS_REF, MODE_SCHWARZ, kWarpAccMax);
+    else if (precision == SQ_FP64) {
+        // the FP64 J/K launches carry the Fock build's large-bound high-L quartets
+        if (kacc <= 2)
+            SQ_WARP_LAUNCH(double, BOYS_FP64, MODE_JK, 2);
+        else if (kacc <= 8)
+            SQ_WARP_LAUNCH(double, BOYS_FP64, MODE_JK, 8);
+        else if (kacc <= 16)
+            SQ_WARP_LAUNCH(double, BOYS_FP64, MODE_JK, 16);
+        else
+            SQ_WARP_LAUNCH(double, BOYS_FP64, MODE_JK, kWarpAccMax);
+    } else if (precision == SQ_FP32)
+        SQ_WARP_LAUNCH(float, BOYS_FP64, MODE_JK, kWarpAccMax);
     else
-        SQ_WARP_LAUNCH(float, BOYS_FP32, MODE_JK);
+        SQ_WARP_LAUNCH(float, BOYS_FP32, MODE_JK, kWarpAccMax);
 #undef SQ_WARP_LAUNCH
     return cudaGetLastError();
 }

@@ -398,37 +398,18 @@ class IntegralEngine:
         # S a quartet with the heaviest ket group can ask for; sub-slot k of S covers
         # primitive pairs [k*n//S, (k+1)*n//S) of its parent and shares its data
         max_np = int(npp.max()) if nslot else 0
-        self.sub_first: dict[int, np.ndarray] = {}
-        sub_pair, sub_npp, sub_pb, sub_ps, sub_hb, sub_code, sub_qsum = [], [], [], [], [], [], []
-        nsub = 0
         la_s = self.l[self.pair_shells[slot_pair, 0]] if nslot else np.zeros(0, np.int32)
         lb_s = self.l[self.pair_shells[slot_pair, 1]] if nslot else np.zeros(0, np.int32)
         E_s = np.array([herm_size(int(a), int(b)) for a, b in zip(la_s, lb_s)], dtype=np.int64)
         # heaviest quartet class a slot can be the bra of: (its pair class | its pair class)
         pc_s = self.pair_class[slot_pair] if nslot else np.zeros(0, np.int64)
         w_s = np.array([CLASS_WEIGHT[screening.quartet_class(int(c), int(c))] for c in pc_s], dtype=np.float64)
-        S = 2
-        while nslot:
-            want = ((npp * max_np * w_s > SPLIT_TARGET * (S // 2)) | (npp >= 4 * S)) & (npp >= S)
-            idx = np.nonzero(want)[0]
-            if len(idx) == 0:
-                break
-            first = np.full(nslot, -1, np.int64)
-            first[idx] = nslot + nsub + S * np.arange(len(idx))
-            self.sub_first[S] = first
-            k = np.tile(np.arange(S), len(idx))
-            par = np.repeat(idx, S)
-            lo = (k * npp[par]) // S
-            hi = ((k + 1) * npp[par]) // S
-            sub_pair.append(slot_pair[par])
-            sub_npp.append(hi - lo)
-            sub_pb.append(pbase[par] + lo * pstride[par])
-            sub_ps.append(pstride[par])
-            sub_hb.append(hbase[par] + lo * E_s[par] * pstride[par])
-            sub_code.append((k << 16) | S)
-            sub_qsum.append(qcum[prim_src_off[par] + hi] - qcum[prim_src_off[par] + lo])
-            nsub += S * len(idx)
-            S *= 2
+        self.sub_first, subs = screening.sub_slot_table(npp, pbase, pstride, hbase, E_s, w_s, qcum, prim_src_off,
+                                                        max_np, SPLIT_TARGET)
+        sub_pair = [slot_pair[subs["parent"]]] if len(subs["parent"]) else []
+        sub_npp, sub_pb, sub_ps, sub_hb = [subs["npp"]], [subs["pbase"]], [subs["pstride"]], [subs["hbase"]]
+        sub_code, sub_qsum = [subs["code"]], [subs["qsum"]]
+        nsub = len(subs["parent"])
         self.nslot_base = nslot
         if nsub:
             slot_pair = np.concatenate([slot_pair] + sub_pair).astype(np.int32)

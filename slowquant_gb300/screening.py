@@ -146,3 +146,55 @@ def expand_host(bra, kst, cnt, ket_list) -> np.ndarray:
     first = np.repeat(np.concatenate([[0], np.cumsum(cnt)[:-1]]), cnt)
     k = np.arange(int(cnt.sum())) - first
     return np.stack([rep_bra, ket_list[starts + k]], axis=1).astype(np.int32)
+
+
+def sub_slot_table(npp, pbase, pstride, hbase, herm_per_prim, weight, qcum, prim_off, max_np: int,
+                   split_target: float):
+    """Sub-slots: chunk k of S (a power of two) of a slot's primitive pairs.
+
+    Sub-slot k of S covers the slot's primitive pairs [k*n//S, (k+1)*n//S)
+    (n = npp of the slot) and points into the slot's data (field-major layout
+    with stride pstride: primitive i at pbase + i*pstride, its Hermite block at
+    hbase + i*herm_per_prim*pstride).  Chunk counts are made for the S a split
+    can ask for: the slot's heaviest quartet (npp * max_np * weight) above
+    split_target * S/2, or chunks of at least 4 primitive pairs (for the
+    per-chunk precision test).  qcum is the prefix sum of the slots' primitive
+    Schwarz factors in slot order (prim_off[s] = start of slot s), which gives
+    each sub-slot's bound sum.
+
+    Returns (first, table): first[S][s] = id of sub-slot 0 of S of slot s (-1:
+    none; ids continue after the nslot slots), and the table's arrays (parent,
+    npp, pbase, pstride, hbase, code = k << 16 | S, qsum).
+    """
+    npp = np.asarray(npp, dtype=np.int64)
+    nslot = len(npp)
+    max_np = int(max_np)
+    first_of = {}
+    cols = {k: [] for k in ("parent", "npp", "pbase", "pstride", "hbase", "code", "qsum")}
+    nsub = 0
+    S = 2
+    while nslot:
+        want = ((npp * max_np * weight > split_target * (S // 2)) | (npp >= 4 * S)) & (npp >= S)
+        idx = np.nonzero(want)[0]
+        if len(idx) == 0:
+            break
+        first = np.full(nslot, -1, np.int64)
+        first[idx] = nslot + nsub + S * np.arange(len(idx))
+        first_of[S] = first
+        k = np.tile(np.arange(S), len(idx))
+        par = np.repeat(idx, S)
+        lo = (k * npp[par]) // S
+        hi = ((k + 1) * npp[par]) // S
+        cols["parent"].append(par)
+        cols["npp"].append(hi - lo)
+        cols["pbase"].append(pbase[par] + lo * pstride[par])
+        cols["pstride"].append(pstride[par])
+        cols["hbase"].append(hbase[par] + lo * herm_per_prim[par] * pstride[par])
+        cols["code"].append((k << 16) | S)
+        cols["qsum"].append(qcum[prim_off[par] + hi] - qcum[prim_off[par] + lo])
+        nsub += S * len(idx)
+        S *= 2
+    dtypes = {"parent": np.int64, "npp": np.int32, "pbase": np.int32, "pstride": np.int32, "hbase": np.int64,
+              "code": np.int64, "qsum": np.float64}
+    table = {k: (np.concatenate(v).astype(dtypes[k]) if v else np.zeros(0, dtypes[k])) for k, v in cols.items()}
+    return first_of, table

@@ -137,3 +137,35 @@ def test_library_exports_every_header_symbol():
     for name in _header_functions():
         assert hasattr(lib, name), name
     assert lib.sq_version() >= 1
+
+
+def test_sub_slot_table_partitions_each_slot():
+    """Sub-slot chunks tile their parent's primitive pairs exactly and carry the right bound sums."""
+    import numpy as np
+
+    from slowquant_gb300 import screening
+
+    rng = np.random.default_rng(11)
+    nslot = 40
+    npp = rng.integers(1, 65, nslot)
+    pstride = rng.integers(1, 9, nslot)
+    pbase = np.cumsum(np.concatenate([[0], npp[:-1] * pstride[:-1]]))
+    E = rng.integers(1, 12, nslot)
+    hbase = np.cumsum(np.concatenate([[0], (npp * E * pstride)[:-1]]))
+    w = rng.uniform(1, 50, nslot)
+    q = rng.uniform(0, 1, int(npp.sum()))
+    qcum = np.concatenate([[0.0], np.cumsum(q)])
+    off = np.concatenate([[0], np.cumsum(npp)[:-1]])
+    first, t = screening.sub_slot_table(npp, pbase, pstride, hbase, E, w, qcum, off, int(npp.max()), 512)
+    assert first, "some slots must be split"
+    for S, f in first.items():
+        for s in np.nonzero(f >= 0)[0]:
+            ids = f[s] - nslot + np.arange(S)
+            assert np.all(t["parent"][ids] == s)
+            assert t["npp"][ids].sum() == npp[s]
+            assert np.all((t["code"][ids] & 0xFFFF) == S) and np.all((t["code"][ids] >> 16) == np.arange(S))
+            lo = np.concatenate([[0], np.cumsum(t["npp"][ids])[:-1]])
+            np.testing.assert_array_equal(t["pbase"][ids], pbase[s] + lo * pstride[s])
+            np.testing.assert_array_equal(t["hbase"][ids], hbase[s] + lo * E[s] * pstride[s])
+            np.testing.assert_allclose(t["qsum"][ids].sum(), q[off[s]:off[s] + npp[s]].sum(), rtol=1e-12)
+            assert npp[s] >= S
