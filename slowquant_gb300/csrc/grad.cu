@@ -21,19 +21,25 @@
 
 namespace sq {
 
-constexpr int kGradWarps = 2;
+constexpr int kGradWarps = 4;
 constexpr int kGHmax = nherm(4 * SQ_LMAX + 1);                                    // R to L + 1
 constexpr int kGWmax = nherm(2 * SQ_LMAX + 1) * ncart(SQ_LMAX) * ncart(SQ_LMAX);  // W'[tuv][cd]
 constexpr int kGGmax = ncart(SQ_LMAX) * ncart(SQ_LMAX) * ncart(SQ_LMAX) * ncart(SQ_LMAX);
 constexpr int kGE = SQ_LMAX + 2;  // 1D tables with indices up to l + 1
 
-struct GradSmem {
-    double rbuf[2][kGHmax];
-    double W[kGWmax];
-    double G[kGGmax];
-    double E[3][kGE][kGE][2 * kGE - 1];
-    double Fs[16];
+// A warp's shared-memory slice, laid out per quartet class (offsets in doubles):
+// two R buffers, W'[cd][h], Gamma'[ab][cd], the three 1D E tables, F_m.  Sizing
+// it per class (instead of for (dd|dd)) lets the light classes keep many more
+// warps resident.
+struct GradLayout {
+    int rbuf;    // entries per R buffer: nherm(L + 1)
+    int W;       // offset of W'
+    int G;       // offset of Gamma'
+    int E;       // offset of the E tables [3][kGE][kGE][2 kGE - 1]
+    int Fs;      // offset of F_m (16)
+    int stride;  // doubles per warp (multiple of 2)
 };
+constexpr int kGEsize = 3 * kGE * kGE * (2 * kGE - 1);
 
 // 1D expansion coefficients E^{ij}_t / E^{00}_0 (integralfunctions.py:9-71).
 template <int NI, int NT>
@@ -88,10 +94,42 @@ __device__ inline double boys_any(int m, double T, const double *tab) {
     return sum * exp(-T);
 }
 
-__global__ void __launch_bounds__(32 * kGradWarps) grad2e_kernel(const EriArgs args, int swap, double *grad) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+// Angular momenta of quartet class qc (bra pair class >= ket pair class).
+inline void grad_class_l(int qc, int &la, int &lb, int &lc, int &ld) {
+    int cb = 0;
+    while ((cb + 1) * (cb + 2) / 2 <= qc) ++cb;
+    const int ck = qc - cb * (cb + 1) / 2;
+    la = 0;
+    while ((la + 1) * (la + 2) / 2 <= cb) ++la;
+    lb = cb - la * (la + 1) / 2;
+    lc = 0;
+    while ((lc + 1) * (lc + 2) / 2 <= ck) ++lc;
+    ld = ck - lc * (lc + 1) / 2;
+}
+
+// Layout for a class in either orientation (the ket-centre pass swaps bra and ket).
+inline GradLayout grad_layout(int la, int lb, int lc, int ld) {
+    const int nab = ncart(la) * ncart(lb), ncd = ncart(lc) * ncart(ld);
+    const int L1 = la + lb + lc + ld + 1;
+    const int w1 = nherm(la + lb + 1) * ncd, w2 = nherm(lc + ld + 1) * nab;
+    GradLayout g;
+    g.rbuf = nherm(L1);
+    g.W = 2 * g.rbuf;
+    g.G = g.W + (w1 > w2 ? w1 : w2);
+    g.E = g.G + nab * ncd;
+    g.Fs = g.E + kGEsize;
+    g.stride = (g.Fs + 16 + 1) / 2 * 2;
+    return g;
+}
+
+__global__ void __launch_bounds__(32 * kGradWarps) grad2e_kernel(const EriArgs args, int swap, double *grad,
+                                                                const GradLayout lay) {
+    extern __shared__ __align__(16) double smem_d[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    GradSmem &sm = reinterpret_cast<GradSmem *>(smem_raw)[warp];
+    double *wbase = smem_d + (long long)warp * lay.stride;
+    double *rbuf0 = wbase, *rbuf1 = wbase + lay.rbuf;
+    double *smW = wbase + lay.W, *smG = wbase + lay.G, *smFs = wbase + lay.Fs;
+    double(*smE)[kGE][kGE][2 * kGE - 1] = reinterpret_cast<double(*)[kGE][kGE][2 * kGE - 1]>(wbase + lay.E);
     __shared__ int s_tuv[kGHmax];
     for (int e = threadIdx.x; e < kGHmax; e += blockDim.x) {
         int n = 0;
@@ -132,7 +170,7 @@ __global__ void __launch_bounds__(32 * kGradWarps) grad2e_kernel(const EriArgs a
         for (int x = lane; x < NAB * NCD; x += 32) {
             const int ab = x / NCD, cd = x - ab * NCD;
             const long long A = oa + ab / NB, B = ob + ab % NB, C = oc + cd / ND, Dd = od + cd % ND;
-            sm.G[x] = 0.5 * m *
+            smG[x] = 0.5 * m *
                       (gload(D + A * n + B) * gload(D + C * n + Dd) -
                        0.25 * (gload(D + A * n + C) * gload(D + B * n + Dd) + gload(D + A * n + Dd) * gload(D + B * n + C)));
         }
@@ -152,8 +190,8 @@ __global__ void __launch_bounds__(32 * kGradWarps) grad2e_kernel(const EriArgs a
             const double Ub = gload(pr.prim + 8 * i + 4);
             if (lane < 3)
                 ecoef_table<kGE, 2 * kGE - 1>(Pv[lane] - gload(Ac + lane), Pv[lane] - gload(Bc + lane), 0.5 / p, la + 1,
-                                             lb + 1, sm.E[lane]);
-            for (int w = lane; w < HAB1 * NCD; w += 32) sm.W[w] = 0.0;
+                                             lb + 1, smE[lane]);
+            for (int w = lane; w < HAB1 * NCD; w += 32) smW[w] = 0.0;
             __syncwarp();
             for (int k = k0; k < k1; ++k) {
                 const double q = gload(pr.prim + 8 * k + 0);
@@ -167,18 +205,18 @@ __global__ void __launch_bounds__(32 * kGradWarps) grad2e_kernel(const EriArgs a
                 if (lane <= L1) {
                     double fac = kTwoPi52 * Ub * Uk * r;
                     for (int j = 0; j < lane; ++j) fac *= -2.0 * alpha;
-                    sm.Fs[lane] = fac * boys_any(lane, T, args.tab64);
+                    smFs[lane] = fac * boys_any(lane, T, args.tab64);
                 }
                 __syncwarp();
-                double *cur = sm.rbuf[0], *nxt = sm.rbuf[1];
-                if (lane == 0) cur[0] = sm.Fs[L1];
+                double *cur = rbuf0, *nxt = rbuf1;
+                if (lane == 0) cur[0] = smFs[L1];
                 __syncwarp();
                 for (int lev = L1 - 1; lev >= 0; --lev) {
                     const int cnt = nherm(L1 - lev);
                     for (int e = lane; e < cnt; e += 32) {
                         double val;
                         if (e == 0) {
-                            val = sm.Fs[lev];
+                            val = smFs[lev];
                         } else {
                             const int tuv = s_tuv[e];
                             const int t = tuv & 255, u = (tuv >> 8) & 255, v = tuv >> 16;
@@ -221,7 +259,7 @@ __global__ void __launch_bounds__(32 * kGradWarps) grad2e_kernel(const EriArgs a
                                 if ((tau + nu + phi) & 1) ev = -ev;
                                 s = fma(ev, cur[herm_index(t + tau, u + nu, v + phi)], s);
                             }
-                    sm.W[w] += s;
+                    smW[w] += s;
                 }
                 __syncwarp();
             }
@@ -242,7 +280,7 @@ __global__ void __launch_bounds__(32 * kGradWarps) grad2e_kernel(const EriArgs a
                             if (raised > 1) continue;
                             const int h = herm_index(t, u, v);
                             double Yv = 0.0;
-                            for (int cd = 0; cd < NCD; ++cd) Yv = fma(sm.W[cd * HAB1 + h], sm.G[ab * NCD + cd], Yv);
+                            for (int cd = 0; cd < NCD; ++cd) Yv = fma(smW[cd * HAB1 + h], smG[ab * NCD + cd], Yv);
                             const int idx3[3] = {t, u, v};
                             for (int dir = 0; dir < 3; ++dir) {
                                 // the other two directions must lie inside their unraised ranges
@@ -254,11 +292,11 @@ __global__ void __launch_bounds__(32 * kGradWarps) grad2e_kernel(const EriArgs a
                                         ok = false;
                                         break;
                                     }
-                                    other *= sm.E[o][a3[o]][b3[o]][idx3[o]];
+                                    other *= smE[o][a3[o]][b3[o]][idx3[o]];
                                 }
                                 if (!ok) continue;
                                 const int td = idx3[dir];
-                                const double (*Ed)[kGE][2 * kGE - 1] = sm.E[dir];
+                                const double (*Ed)[kGE][2 * kGE - 1] = smE[dir];
                                 double dA = 2.0 * al * Ed[a3[dir] + 1][b3[dir]][td];
                                 if (a3[dir] > 0 && td <= a3[dir] - 1 + b3[dir]) dA -= a3[dir] * Ed[a3[dir] - 1][b3[dir]][td];
                                 double dB = 2.0 * be * Ed[a3[dir]][b3[dir] + 1][td];
@@ -489,13 +527,24 @@ extern "C" int sq_grad_2e(const sq_basis *basis, const sq_pairs *pairs, const sq
     a.D = D;
     a.quartets = reinterpret_cast<const int2 *>(quartets->pairs);
     a.nq = quartets->nquartet;
-    const size_t sz = sizeof(GradSmem) * kGradWarps;
-    cudaError_t e = cudaFuncSetAttribute(grad2e_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sz);
+    // one launch per quartet class and orientation, each with its own shared-memory layout
+    const size_t full = (size_t)grad_layout(SQ_LMAX, SQ_LMAX, SQ_LMAX, SQ_LMAX).stride * sizeof(double) * kGradWarps;
+    cudaError_t e = cudaFuncSetAttribute(grad2e_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)full);
     if (e != cudaSuccess) return set_error(SQ_ERR_CUDA, "sq_grad_2e: %s", cudaGetErrorString(e));
-    long long blocks = (a.nq + kGradWarps - 1) / kGradWarps;
-    if (blocks > 152LL * 64) blocks = 152LL * 64;
-    for (int swap = 0; swap < 2; ++swap)
-        grad2e_kernel<<<(unsigned)blocks, 32 * kGradWarps, sz, (cudaStream_t)stream>>>(a, swap, grad);
+    for (int c = 0; c < SQ_MAX_QCLASS; ++c) {
+        const long long nq = quartets->class_off[c + 1] - quartets->class_off[c];
+        if (nq <= 0) continue;
+        int la, lb, lc, ld;
+        grad_class_l(c, la, lb, lc, ld);
+        const GradLayout lay = grad_layout(la, lb, lc, ld);
+        a.quartets = reinterpret_cast<const int2 *>(quartets->pairs) + quartets->class_off[c];
+        a.nq = nq;
+        const size_t sz = (size_t)lay.stride * sizeof(double) * kGradWarps;
+        long long blocks = (nq + kGradWarps - 1) / kGradWarps;
+        if (blocks > 152LL * 64) blocks = 152LL * 64;
+        for (int swap = 0; swap < 2; ++swap)
+            grad2e_kernel<<<(unsigned)blocks, 32 * kGradWarps, sz, (cudaStream_t)stream>>>(a, swap, grad, lay);
+    }
     return check_launch("sq_grad_2e");
 }
 
