@@ -128,8 +128,8 @@ typedef struct sq_slots {
     /* optional sub-slots (NULL: every slot is whole).  sub[s] = 0 for a whole
      * slot; (k << 16) | S for chunk k of S of a slot's primitive pairs (its
      * npp/pbase/hbase then describe that chunk; pair[s] is the parent's pair).
-     * Only J/K quartet lists may name sub-slots, as bra entries: J and K are
-     * linear in the integrals, so the S partial quartets add up to the whole.
+     * Only J/K quartet lists may name sub-slots (bra or ket entries): J and K
+     * are linear in the integrals, so the partial quartets add up to the whole.
      * Dense-tensor, Schwarz and gradient lists must name whole slots. */
     const int *sub;
 } sq_slots;
@@ -161,6 +161,11 @@ const char *sq_last_error(void);
  * take the next streams of a pool of 16, so calls issued concurrently from
  * different caller streams run side by side. */
 #define SQ_OPT_JK_STREAMS 2
+/* SQ_OPT_FP64_UNROLLED_HIGH: bit mask over quartet classes; a set bit runs
+ * that class's FP64 J/K launches on its per-thread kernel where one exists
+ * ((dp|pp) 12, (dp|ds) 13, (dd|ss) 15, (dd|ps) 16), a clear bit on the
+ * generic warp kernel.  Default: all four. */
+#define SQ_OPT_FP64_UNROLLED_HIGH 3
 int sq_set_option(int key, long long value);
 long long sq_get_option(int key);
 

@@ -40,10 +40,25 @@ static const eri_launcher kLaunchersF32[SQ_MAX_QCLASS] = {
     launch_qc_14_f32, launch_qc_15_f32, launch_qc_16_f32, launch_qc_17_f32, launch_qc_18_f32, nullptr, nullptr,
 };
 
+cudaError_t launch_qc_12_f64(const EriArgs &, int, int, cudaStream_t);
+cudaError_t launch_qc_13_f64(const EriArgs &, int, int, cudaStream_t);
+cudaError_t launch_qc_15_f64(const EriArgs &, int, int, cudaStream_t);
+cudaError_t launch_qc_16_f64(const EriArgs &, int, int, cudaStream_t);
+
+// FP64 (SQ_FP64) per-thread kernels beyond the all-precision ones, for classes
+// with L >= 4 whose register blocks spill partly to local memory but still
+// outrun the generic warp kernel: (dp|pp), (dp|ds), (dd|ss), (dd|ps).
+static const eri_launcher kLaunchersF64[SQ_MAX_QCLASS] = {
+    nullptr,          nullptr,          nullptr, nullptr,          nullptr,          nullptr, nullptr,
+    nullptr,          nullptr,          nullptr, nullptr,          nullptr,          launch_qc_12_f64,
+    launch_qc_13_f64, nullptr,          launch_qc_15_f64, launch_qc_16_f64, nullptr, nullptr, nullptr, nullptr,
+};
+
 // Per-thread (fully unrolled) J/K kernels exist for the light classes (L <= 4,
-// except (dd|ss)) in every precision, and for classes 12-18 in SQ_FP32; every
-// other class/precision, and every dense-tensor or Schwarz launch, runs on the
-// generic warp kernel.  SQ_OPT_GENERIC_MIN_L = 0 sends everything to it.
+// except (dd|ss)) in every precision, for classes 12, 13, 15, 16 in SQ_FP64 and
+// for classes 12-18 in SQ_FP32; every other class/precision, and every
+// dense-tensor or Schwarz launch, runs on the generic warp kernel.
+// SQ_OPT_GENERIC_MIN_L = 0 sends everything to it.
 static const eri_launcher kLaunchers[SQ_MAX_QCLASS] = {
     launch_qc_0, launch_qc_1, launch_qc_2, launch_qc_3, launch_qc_4, launch_qc_5, launch_qc_6,
     launch_qc_7, launch_qc_8, launch_qc_9, launch_qc_10, launch_qc_11, nullptr, nullptr,
@@ -67,6 +82,9 @@ static void quartet_class_l(int qc, int &la, int &lb, int &lc, int &ld) {
 
 // Classes with la+lb+lc+ld >= g_generic_min_l use the warp kernel.
 static int g_generic_min_l = 5;
+// Bit c set: the FP64 J/K launches of class c run on its kLaunchersF64 kernel,
+// else on the warp kernel (option SQ_OPT_FP64_UNROLLED_HIGH).
+static long long g_fp64_unrolled_high = (1LL << 12) | (1LL << 13) | (1LL << 15) | (1LL << 16);
 
 // Autotuned launch shapes per (quartet class, precision); threads 0 = default.
 struct LaunchCfg {
@@ -149,6 +167,9 @@ static cudaError_t launch_class(EriArgs &args, const sq_quartets *qs, int c, int
     if (mode == MODE_JK && L < g_generic_min_l) unrolled = kLaunchers[c];
     if (mode == MODE_JK && precision == SQ_FP32 && kLaunchersF32[c] != nullptr && g_generic_min_l > 0)
         unrolled = kLaunchersF32[c];
+    if (mode == MODE_JK && precision == SQ_FP64 && kLaunchersF64[c] != nullptr && g_generic_min_l > 0 &&
+        ((g_fp64_unrolled_high >> c) & 1))
+        unrolled = kLaunchersF64[c];
     if (unrolled != nullptr) return unrolled(args, mode, precision, stream);
     return launch_eri_warp(args, WarpClass{la, lb, lc, ld}, mode, precision, stream);
 }
@@ -213,6 +234,12 @@ extern "C" int sq_set_option(int key, long long value) {
         g_jk_streams = (int)value;
         return SQ_OK;
     }
+    if (key == SQ_OPT_FP64_UNROLLED_HIGH) {
+        if (value < 0 || value >= (1LL << SQ_MAX_QCLASS))
+            return set_error(SQ_ERR_ARG, "sq_set_option: class mask out of range");
+        g_fp64_unrolled_high = value;
+        return SQ_OK;
+    }
     if (key == SQ_OPT_GENERIC_MIN_L) {
         if (value < 0) return set_error(SQ_ERR_ARG, "sq_set_option: negative L");
         g_generic_min_l = (int)value;
@@ -233,6 +260,7 @@ extern "C" int sq_set_launch_config(int qclass, int precision, int threads, long
 extern "C" long long sq_get_option(int key) {
     if (key == SQ_OPT_GENERIC_MIN_L) return g_generic_min_l;
     if (key == SQ_OPT_JK_STREAMS) return g_jk_streams;
+    if (key == SQ_OPT_FP64_UNROLLED_HIGH) return g_fp64_unrolled_high;
     return -1;
 }
 

@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(const EriArgs args) {
             double m = 8.0;
             if (sa == sb) m *= 0.5;
             if (sc == sd) m *= 0.5;
-            if (pairP == pairQ) m *= 0.5;  // bra sub-slots of a pair count as that pair
+            if (pairP == pairQ) m *= 0.5;  // sub-slots of a pair count as that pair
             const R wJ = R(0.5 * m), wK = R(0.25 * m);
             const int nd = args.nd > 1 ? args.nd : 1;
             for (int di = 0; di < nd; ++di) {
@@ -490,6 +490,20 @@ cudaError_t launch_eri_class(const EriArgs &args, int mode, int precision, cudaS
         eri_class_kernel<LA, LB, LC, LD, float, BOYS_FP64, MODE_JK><<<(int)blocks, threads, 0, stream>>>(args);
     else
         eri_class_kernel<LA, LB, LC, LD, float, BOYS_FP32, MODE_JK><<<(int)blocks, threads, 0, stream>>>(args);
+    return cudaGetLastError();
+}
+
+// FP64-only launcher (SQ_FP64) for a class whose FP32 variants have their own TU.
+template <int LA, int LB, int LC, int LD>
+cudaError_t launch_eri_class_f64(const EriArgs &args, int mode, int precision, cudaStream_t stream) {
+    (void)mode;
+    (void)precision;
+    if (args.nq <= 0) return cudaSuccess;
+    const int threads = args.cfg_threads > 0 ? args.cfg_threads : 128;
+    long long blocks = (args.nq + threads - 1) / threads;
+    const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : 152LL * 16 * 8;
+    if (blocks > cap) blocks = cap;
+    eri_class_kernel<LA, LB, LC, LD, double, BOYS_FP64, MODE_JK><<<(int)blocks, threads, 0, stream>>>(args);
     return cudaGetLastError();
 }
 

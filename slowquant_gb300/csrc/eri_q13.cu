@@ -9,4 +9,10 @@ cudaError_t launch_qc_13_f32(const EriArgs &a, int mode, int prec, cudaStream_t 
     return launch_eri_class_f32<2, 1, 2, 0>(a, mode, prec, s);
 }
 
+// FP64 per-thread variant: its register block spills to local memory, which
+// still beats the generic warp kernel's lane utilisation for this class.
+cudaError_t launch_qc_13_f64(const EriArgs &a, int mode, int prec, cudaStream_t s) {
+    return launch_eri_class_f64<2, 1, 2, 0>(a, mode, prec, s);
+}
+
 }  // namespace sq

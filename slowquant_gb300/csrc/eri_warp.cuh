@@ -151,14 +151,20 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
         const int Q = args.use_slots ? gload(args.slots.pair + pq.y) : pq.y;
         const int i0 = gload(pr.pp_off + P), i1 = gload(pr.pp_off + P + 1);
         const int k0 = gload(pr.pp_off + Q), k1 = gload(pr.pp_off + Q + 1);
-        // a bra sub-slot (chunk k of S) covers bra primitives [ib0, ib1) of the pair
-        int ib0 = i0, ib1 = i1;
+        // a sub-slot (chunk k of S) covers primitives [k np / S, (k+1) np / S) of its pair
+        int ib0 = i0, ib1 = i1, kb0 = k0, kb1 = k1;
         if (args.use_slots && args.slots.sub) {
             const int code = gload(args.slots.sub + pq.x);
             if (code) {
                 const int S = code & 0xffff, kc = code >> 16, np = i1 - i0;
                 ib0 = i0 + (kc * np) / S;
                 ib1 = i0 + ((kc + 1) * np) / S;
+            }
+            const int codek = gload(args.slots.sub + pq.y);
+            if (codek) {
+                const int S = codek & 0xffff, kc = codek >> 16, np = k1 - k0;
+                kb0 = k0 + (kc * np) / S;
+                kb1 = k0 + ((kc + 1) * np) / S;
             }
         }
         const R *hb = herm + gload(pr.herm_off + P);
@@ -172,7 +178,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
             const R Px = gload(prim + 8 * i + 1), Py = gload(prim + 8 * i + 2), Pz = gload(prim + 8 * i + 3);
             const R Ub = gload(prim + 8 * i + 4);
             for (int w = lane; w < NW; w += 32) sm.W[w] = R(0);
-            for (int k = k0; k < k1; ++k) {
+            for (int k = kb0; k < kb1; ++k) {
                 const R q = gload(prim + 8 * k + 0);
                 const R X = Px - gload(prim + 8 * k + 1);
                 const R Y = Py - gload(prim + 8 * k + 2);

@@ -499,8 +499,9 @@ class IntegralEngine:
 
         FP64 quartets of the per-thread classes (0-11) are cut into S chunks of
         their bra's primitive pairs (sorted by descending factor, about 4-8 per
-        chunk, more when the quartet is heavy), and each chunk is placed by its
-        own bound qsum[chunk] * qsum[ket]; FP32 quartets stay whole.
+        chunk, more when the quartet is heavy), kets are cut the same way where
+        a ket straddles the threshold, and each (bra chunk, ket chunk) is placed
+        by its own bound; FP32 quartets stay whole.
         """
         t64, t32 = lists
         q32 = self._expand(t32, ket_list, 18)
@@ -529,9 +530,9 @@ class IntegralEngine:
                     first = self.sub_first[S][pairs[:, 0]]
                     chunk = np.concatenate([np.stack([(first + k).astype(np.int32), pairs[:, 1]], 1)
                                             for k in range(S)])
-                big = self.slot_qsum[chunk[:, 0]] * self.slot_qsum[chunk[:, 1]] >= tau
-                keep64[c].append(chunk[big])
-                move32[c].append(chunk[~big])
+                k64, k32 = self._ket_chunks(chunk, tau)
+                keep64[c].append(k64)
+                move32[c].append(k32)
         # FP64 list: whole-quartet blocks of the warp classes (device expand) and
         # the kept chunks; FP32 list: the quartet-level FP32 list plus the moved chunks
         q64w = self._expand(whole64, ket_list, -1)
@@ -552,6 +553,49 @@ class IntegralEngine:
             return QuartetList(pairs, off)
 
         return [merge(q64w, keep64), merge(q32, move32)]
+
+    def _ket_chunks(self, entries: np.ndarray, tau: float):
+        """Partition (bra, ket) entries by bound into (FP64, FP32) entries.
+
+        An entry whose whole ket passes or fails the test stays whole; otherwise
+        its ket is cut into chunks of about 4-8 primitive pairs (ket sub-slots)
+        and each chunk is placed by qsum[bra] * qsum[ket chunk].
+        """
+        qs = self.slot_qsum
+        qb = qs[entries[:, 0]]
+        whole = qb * qs[entries[:, 1]]
+        # the largest and smallest ket chunk bounds decide whether the ket must be cut
+        npp = self.slot_npp
+        kslot = entries[:, 1]
+        nk = npp[kslot].astype(np.int64)
+        Sk = np.ones(len(entries), np.int64)
+        for S in sorted(self.sub_first):
+            ok = (nk >= 8 * S) & (self.sub_first[S][kslot] >= 0)
+            Sk[ok] = S
+        out64, out32 = [], []
+        one = Sk == 1
+        big = whole >= tau
+        out64.append(entries[one & big])
+        out32.append(entries[one & ~big])
+        for S in sorted(set(Sk[~one].tolist())):
+            sel = np.nonzero(Sk == S)[0]
+            first = self.sub_first[S][kslot[sel]]
+            kc = first[:, None] + np.arange(S)[None, :]  # ket chunk ids per entry
+            b = qb[sel, None] * qs[kc]
+            all_big = (b >= tau).all(axis=1)
+            all_small = (b < tau).all(axis=1)
+            out64.append(entries[sel[all_big]])
+            out32.append(entries[sel[all_small]])
+            mix = ~(all_big | all_small)
+            if mix.any():
+                bras = np.repeat(entries[sel[mix], 0], S)
+                kets = kc[mix].ravel()
+                bm = b[mix].ravel() >= tau
+                pairs = np.stack([bras, kets], 1).astype(np.int32)
+                out64.append(pairs[bm])
+                out32.append(pairs[~bm])
+        cat = lambda xs: np.concatenate(xs).astype(np.int32) if xs else np.zeros((0, 2), np.int32)  # noqa: E731
+        return cat(out64), cat(out32)
 
     def _split_tasks(self, tasks: dict, ket_list: np.ndarray, split_max_class: int) -> dict:
         """Bra slot ids of every task block, heavy blocks replaced by their sub-slot chunks."""

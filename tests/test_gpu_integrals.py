@@ -281,3 +281,24 @@ def test_chunk_level_mixed_precision():
     p = c64.pairs[: int(c64.class_off[12])].cpu().numpy()
     assert np.all(eng.slot_qsum[p[:, 0]] * eng.slot_qsum[p[:, 1]] >= 1e-4)
     assert np.max(np.abs(Jm - J0)) < 1e-6
+
+
+def test_chunk_lists_partition_exactly_in_fp64():
+    """The chunk lists (bra and ket sub-slots) run both in FP64 reproduce the FP64 J/K,
+    on the per-thread kernels and on the generic warp kernel."""
+    import torch
+
+    from slowquant_gb300 import _lib, systems
+
+    eng = _engine(systems.water_cluster(3, 6.0, seed=3), "cc-pvdz", "angstrom")
+    D = torch.tensor(_random_density(eng.nbf, 9), dtype=torch.float64, device="cuda")
+    J0, K0 = (x.cpu().numpy() for x in eng.jk(D, 1e-12, "fp64"))
+    c64, c32 = eng.quartets(1e-12, 1e-4, chunks=True)
+    assert (eng.slot_sub[c64.pairs[: c64.nquartet, 1].cpu().numpy()] != 0).any()  # some kets were cut
+    for min_l in (5, 0):
+        _lib.lib().sq_set_option(_lib.SQ_OPT_GENERIC_MIN_L, min_l)
+        Ja, Ka = eng.jk_accumulate(D, [c64, c32], ["fp64", "fp64"])
+        J = (0.5 * (Ja + Ja.T)).cpu().numpy()
+        K = (0.5 * (Ka + Ka.T)).cpu().numpy()
+        np.testing.assert_allclose(J, J0, atol=1e-11)
+        np.testing.assert_allclose(K, K0, atol=1e-11)

@@ -156,3 +156,25 @@ def test_ao_to_mo_transforms_match_einsum(gpu_lib, golden_energies):
     Ca = C[:, 2:9]
     np.testing.assert_allclose(two_electron_integral_transform(Ca, g),
                                np.einsum("ai,bj,ck,dl,abcd->ijkl", Ca, Ca, Ca, Ca, g, optimize=True), atol=1e-11)
+
+
+H6_BOHR = ";".join(f"H   {float(i):.12f}   0.000000000000   0.000000000000" for i in range(6))
+
+
+def _h6_tensor(threshold):
+    import slowquant_gb300.SlowQuant as sq
+
+    A = sq.SlowQuant()
+    A.set_molecule(H6_BOHR, distance_unit="bohr")
+    A.set_basis_set("dzp")
+    A.integral.cauchy_schwarz_threshold = threshold
+    return A.integral.electron_repulsion_tensor
+
+
+def test_cauchy_schwarz_inequality_like_reference(gpu_lib):
+    """The reference's tests/test_integral.py case: H6 chain in DZP, screened tensors stay
+    within the threshold of the (almost) unscreened one, and a huge threshold gives zeros."""
+    ref = _h6_tensor(1e-20)
+    np.testing.assert_allclose(_h6_tensor(1e-8), ref, atol=1e-8)
+    np.testing.assert_allclose(_h6_tensor(1e-3), ref, atol=1e-3)
+    np.testing.assert_allclose(_h6_tensor(1e10), np.zeros(ref.shape), atol=1e-8)
