@@ -138,7 +138,7 @@ def class_work(eng, ql, precision: str = "fp64") -> dict:
     """Per quartet class: contracted quartets, primitive quartets, model FLOPs.
 
     Primitive quartets are the ones the launch computes: the per-thread class
-    kernels (classes 0-13, 15, 16, and 12-18 in FP32) loop over the slots' screened
+    kernels (classes 0-18) loop over the slots' screened
     primitive pairs, the generic warp kernel over all of a pair's primitives.
     """
     import torch
@@ -158,7 +158,7 @@ def class_work(eng, ql, precision: str = "fp64") -> dict:
         a, b = int(ql.class_off[c]), int(ql.class_off[c + 1])
         if b == a:
             continue
-        per_thread = c < 12 or c in (12, 13, 15, 16) or (precision != "fp64" and c <= 18)
+        per_thread = c <= 18
         npp = npp_slot if per_thread else npp_all
         seg = ql.pairs[a:b].long()
         nprim = int((npp[seg[:, 0]] * npp[seg[:, 1]]).sum())

@@ -163,8 +163,8 @@ const char *sq_last_error(void);
 #define SQ_OPT_JK_STREAMS 2
 /* SQ_OPT_FP64_UNROLLED_HIGH: bit mask over quartet classes; a set bit runs
  * that class's FP64 J/K launches on its per-thread kernel where one exists
- * ((dp|pp) 12, (dp|ds) 13, (dd|ss) 15, (dd|ps) 16), a clear bit on the
- * generic warp kernel.  Default: all four. */
+ * (classes 12-18, (dp|pp) to (dd|ds)), a clear bit on the generic warp
+ * kernel.  Default: classes 12-18. */
 #define SQ_OPT_FP64_UNROLLED_HIGH 3
 int sq_set_option(int key, long long value);
 long long sq_get_option(int key);

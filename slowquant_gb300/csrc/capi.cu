@@ -40,24 +40,24 @@ static const eri_launcher kLaunchersF32[SQ_MAX_QCLASS] = {
     launch_qc_14_f32, launch_qc_15_f32, launch_qc_16_f32, launch_qc_17_f32, launch_qc_18_f32, nullptr, nullptr,
 };
 
-cudaError_t launch_qc_12_f64(const EriArgs &, int, int, cudaStream_t);
-cudaError_t launch_qc_13_f64(const EriArgs &, int, int, cudaStream_t);
-cudaError_t launch_qc_15_f64(const EriArgs &, int, int, cudaStream_t);
-cudaError_t launch_qc_16_f64(const EriArgs &, int, int, cudaStream_t);
+#define DECL64(QC) cudaError_t launch_qc_##QC##_f64(const EriArgs &, int, int, cudaStream_t);
+DECL64(12) DECL64(13) DECL64(14) DECL64(15) DECL64(16) DECL64(17) DECL64(18)
+#undef DECL64
 
-// FP64 (SQ_FP64) per-thread kernels beyond the all-precision ones, for classes
-// with L >= 4 whose register blocks spill partly to local memory but still
-// outrun the generic warp kernel: (dp|pp), (dp|ds), (dd|ss), (dd|ps).
+// FP64 (SQ_FP64) per-thread kernels of classes 12-18, (dp|pp) to (dd|ds): their
+// register blocks spill partly to local memory, and they still outrun the
+// generic warp kernel.
 static const eri_launcher kLaunchersF64[SQ_MAX_QCLASS] = {
-    nullptr,          nullptr,          nullptr, nullptr,          nullptr,          nullptr, nullptr,
-    nullptr,          nullptr,          nullptr, nullptr,          nullptr,          launch_qc_12_f64,
-    launch_qc_13_f64, nullptr,          launch_qc_15_f64, launch_qc_16_f64, nullptr, nullptr, nullptr, nullptr,
+    nullptr,          nullptr,          nullptr,          nullptr,          nullptr,          nullptr,
+    nullptr,          nullptr,          nullptr,          nullptr,          nullptr,          nullptr,
+    launch_qc_12_f64, launch_qc_13_f64, launch_qc_14_f64, launch_qc_15_f64, launch_qc_16_f64, launch_qc_17_f64,
+    launch_qc_18_f64, nullptr,          nullptr,
 };
 
 // Per-thread (fully unrolled) J/K kernels exist for the light classes (L <= 4,
-// except (dd|ss)) in every precision, for classes 12, 13, 15, 16 in SQ_FP64 and
-// for classes 12-18 in SQ_FP32; every other class/precision, and every
-// dense-tensor or Schwarz launch, runs on the generic warp kernel.
+// except (dd|ss)) in every precision, and for classes 12-18 in SQ_FP64 and
+// SQ_FP32; every other class/precision, and every dense-tensor or Schwarz
+// launch, runs on the generic warp kernel.
 // SQ_OPT_GENERIC_MIN_L = 0 sends everything to it.
 static const eri_launcher kLaunchers[SQ_MAX_QCLASS] = {
     launch_qc_0, launch_qc_1, launch_qc_2, launch_qc_3, launch_qc_4, launch_qc_5, launch_qc_6,
@@ -84,7 +84,7 @@ static void quartet_class_l(int qc, int &la, int &lb, int &lc, int &ld) {
 static int g_generic_min_l = 5;
 // Bit c set: the FP64 J/K launches of class c run on its kLaunchersF64 kernel,
 // else on the warp kernel (option SQ_OPT_FP64_UNROLLED_HIGH).
-static long long g_fp64_unrolled_high = (1LL << 12) | (1LL << 13) | (1LL << 15) | (1LL << 16);
+static long long g_fp64_unrolled_high = 0x7FLL << 12;  // classes 12-18
 
 // Autotuned launch shapes per (quartet class, precision); threads 0 = default.
 struct LaunchCfg {

@@ -1,6 +1,6 @@
 // eri_q17.cu -- per-thread J/K kernel of quartet class (dd|pp), FP32 integral
-// arithmetic with the FP64 Boys recursion only (its FP64 and all-FP32-Boys launches
-// run on the generic warp kernel).  The dispatch table in capi.cu calls this launcher.
+// arithmetic with the FP64 Boys recursion only (its all-FP32-Boys launches run on the
+// generic warp kernel; FP64 is in eri_q17_f64.cu).  The dispatch table in capi.cu calls this launcher.
 #include "eri.cuh"
 
 namespace sq {
