@@ -43,26 +43,36 @@ def prefix_counts(x: np.ndarray, qk: np.ndarray, thr: float) -> np.ndarray:
         lim = np.where(x > 0, thr / np.where(x > 0, x, 1.0), np.inf)
     cnt = np.searchsorted(-qk, -lim, side="right").astype(np.int64)
     # exact product test at the boundary, the comparison the reference uses
+    # (the division above can round either way by one position)
     for _ in range(4):
-        dec = (cnt > 0) & (x * qk[np.clip(cnt - 1, 0, n - 1)] < thr)
-        cnt = np.where(dec, cnt - 1, cnt)
-        inc = (cnt < n) & (x * qk[np.clip(cnt, 0, n - 1)] >= thr)
-        cnt = np.where(inc, cnt + 1, cnt)
+        last = qk[np.maximum(cnt - 1, 0)]
+        dec = (cnt > 0) & (x * last < thr)
+        nxt = qk[np.minimum(cnt, n - 1)]
+        inc = (cnt < n) & (x * nxt >= thr)
+        if not (dec.any() or inc.any()):
+            break
+        cnt = cnt - dec + inc
     return cnt
 
 
 def pair_groups(pair_class: np.ndarray, npa: np.ndarray, npb: np.ndarray, q: np.ndarray):
-    """[(class, member pair indices sorted by descending q)], ordered by (class, npa, npb)."""
-    keys = np.stack([pair_class, npa, npb], axis=1)
-    if len(keys) == 0:
+    """[(class, member pair indices sorted by descending q)], ordered by (class, npa, npb).
+
+    One stable sort by (class, npa, npb, -q), then a split at the key changes
+    (O(n log n); many thousands of groups occur in a batch of molecules).
+    """
+    pair_class = np.asarray(pair_class)
+    npa = np.asarray(npa)
+    npb = np.asarray(npb)
+    q = np.asarray(q, dtype=np.float64)
+    n = len(pair_class)
+    if n == 0:
         return []
-    uniq = np.unique(keys, axis=0)
-    groups = []
-    for k in uniq:
-        idx = np.nonzero((keys == k).all(axis=1))[0]
-        idx = idx[np.argsort(-q[idx], kind="stable")]
-        groups.append((int(k[0]), idx.astype(np.int32)))
-    return groups
+    order = np.lexsort((np.arange(n), -q, npb, npa, pair_class))
+    kc, ka, kb = pair_class[order], npa[order], npb[order]
+    change = np.nonzero((kc[1:] != kc[:-1]) | (ka[1:] != ka[:-1]) | (kb[1:] != kb[:-1]))[0] + 1
+    bounds = np.concatenate([[0], change, [n]])
+    return [(int(kc[bounds[i]]), order[bounds[i]:bounds[i + 1]].astype(np.int32)) for i in range(len(bounds) - 1)]
 
 
 def build_tasks(pair_class, npa, npb, q, threshold: float, fp32_threshold: float | None = None):
