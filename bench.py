@@ -396,7 +396,7 @@ def gpu_arm(args) -> None:
 
     # primitive-chunk granularity of the same precision test (beside the headline)
     chunk_modes = []
-    for tau in (FP32_THR, 1e-3):
+    for tau in (FP32_THR, 1e-3, 1e-2):
         eng.fock(H, D, SCREEN, "mixed_chunk", tau)
         ms_c = float(np.median(time_events(torch, lambda: eng.fock(H, D, SCREEN, "mixed_chunk", tau), 5, flush)))
         Fc = eng.fock(H, D, SCREEN, "mixed_chunk", tau)

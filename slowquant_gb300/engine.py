@@ -48,6 +48,8 @@ PRIM_SCREEN = 1e-17
 # split over its bra primitives (a class's primitive quartet weighs its model
 # FLOPs over those of (ss|ss))
 SPLIT_TARGET = 512
+# primitive pairs per chunk (at least) in the per-chunk precision mode
+CHUNK_MIN = 2
 _W_SSSS = flops.flops_per_primitive_quartet(0, 0, 0, 0)
 CLASS_WEIGHT = [flops.flops_per_primitive_quartet(*flops.quartet_class_l(c)) / _W_SSSS
                 for c in range(screening.NQCLASS)]
@@ -405,7 +407,7 @@ class IntegralEngine:
         pc_s = self.pair_class[slot_pair] if nslot else np.zeros(0, np.int64)
         w_s = np.array([CLASS_WEIGHT[screening.quartet_class(int(c), int(c))] for c in pc_s], dtype=np.float64)
         self.sub_first, subs = screening.sub_slot_table(npp, pbase, pstride, hbase, E_s, w_s, qcum, prim_src_off,
-                                                        max_np, SPLIT_TARGET)
+                                                        max_np, SPLIT_TARGET, CHUNK_MIN)
         sub_pair = [slot_pair[subs["parent"]]] if len(subs["parent"]) else []
         sub_npp, sub_pb, sub_ps, sub_hb = [subs["npp"]], [subs["pbase"]], [subs["pstride"]], [subs["hbase"]]
         sub_code, sub_qsum = [subs["code"]], [subs["qsum"]]
@@ -498,8 +500,8 @@ class IntegralEngine:
         """(FP64, FP32) lists with the precision test per bra primitive chunk.
 
         FP64 quartets of the per-thread classes (0-11) are cut into S chunks of
-        their bra's primitive pairs (sorted by descending factor, about 4-8 per
-        chunk, more when the quartet is heavy), kets are cut the same way where
+        their bra's primitive pairs (sorted by descending factor, CHUNK_MIN to
+        2 CHUNK_MIN per chunk, more when the quartet is heavy), kets are cut the same way where
         a ket straddles the threshold, and each (bra chunk, ket chunk) is placed
         by its own bound; FP32 quartets stay whole.
         """
@@ -520,7 +522,7 @@ class IntegralEngine:
                 cost = nb * int(npp[ket_slots[st[0]]]) * CLASS_WEIGHT[c]
                 S = 1
                 while (2 * S) in self.sub_first and self.sub_first[2 * S][slots[0]] >= 0 and \
-                        (nb >= 8 * S or cost > SPLIT_TARGET * S):
+                        (nb >= 2 * CHUNK_MIN * S or cost > SPLIT_TARGET * S):
                     S *= 2
                 pairs = screening.expand_host(slots.astype(np.int32), st.astype(np.int32), n.astype(np.int64),
                                               ket_slots)
@@ -558,7 +560,7 @@ class IntegralEngine:
         """Partition (bra, ket) entries by bound into (FP64, FP32) entries.
 
         An entry whose whole ket passes or fails the test stays whole; otherwise
-        its ket is cut into chunks of about 4-8 primitive pairs (ket sub-slots)
+        its ket is cut into chunks of CHUNK_MIN to 2 CHUNK_MIN primitive pairs (ket sub-slots)
         and each chunk is placed by qsum[bra] * qsum[ket chunk].
         """
         qs = self.slot_qsum
@@ -570,7 +572,7 @@ class IntegralEngine:
         nk = npp[kslot].astype(np.int64)
         Sk = np.ones(len(entries), np.int64)
         for S in sorted(self.sub_first):
-            ok = (nk >= 8 * S) & (self.sub_first[S][kslot] >= 0)
+            ok = (nk >= 2 * CHUNK_MIN * S) & (self.sub_first[S][kslot] >= 0)
             Sk[ok] = S
         out64, out32 = [], []
         one = Sk == 1

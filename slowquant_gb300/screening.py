@@ -159,7 +159,7 @@ def expand_host(bra, kst, cnt, ket_list) -> np.ndarray:
 
 
 def sub_slot_table(npp, pbase, pstride, hbase, herm_per_prim, weight, qcum, prim_off, max_np: int,
-                   split_target: float):
+                   split_target: float, min_chunk: int = 4):
     """Sub-slots: chunk k of S (a power of two) of a slot's primitive pairs.
 
     Sub-slot k of S covers the slot's primitive pairs [k*n//S, (k+1)*n//S)
@@ -167,8 +167,8 @@ def sub_slot_table(npp, pbase, pstride, hbase, herm_per_prim, weight, qcum, prim
     with stride pstride: primitive i at pbase + i*pstride, its Hermite block at
     hbase + i*herm_per_prim*pstride).  Chunk counts are made for the S a split
     can ask for: the slot's heaviest quartet (npp * max_np * weight) above
-    split_target * S/2, or chunks of at least 4 primitive pairs (for the
-    per-chunk precision test).  qcum is the prefix sum of the slots' primitive
+    split_target * S/2, or chunks of at least min_chunk primitive pairs (for
+    the per-chunk precision test).  qcum is the prefix sum of the slots' primitive
     Schwarz factors in slot order (prim_off[s] = start of slot s), which gives
     each sub-slot's bound sum.
 
@@ -184,7 +184,7 @@ def sub_slot_table(npp, pbase, pstride, hbase, herm_per_prim, weight, qcum, prim
     nsub = 0
     S = 2
     while nslot:
-        want = ((npp * max_np * weight > split_target * (S // 2)) | (npp >= 4 * S)) & (npp >= S)
+        want = ((npp * max_np * weight > split_target * (S // 2)) | (npp >= min_chunk * S)) & (npp >= S)
         idx = np.nonzero(want)[0]
         if len(idx) == 0:
             break
