@@ -517,6 +517,13 @@ def batch_arm(args) -> None:
     torch.cuda.synchronize()
     setup_s = time.time() - t0
     res = {}
+    # launch shapes of every class and precision from the project's autotuner,
+    # tuned once on this batch's lists (the mixed lists include the FP64 ones)
+    from slowquant_gb300 import autotune
+
+    t0 = time.time()
+    tuning = BatchSCF(be, "mixed").autotune()
+    tune_s = time.time() - t0
     for prec in ("fp64", "mixed"):
         t0 = time.time()
         scf = BatchSCF(be, prec)
@@ -547,8 +554,10 @@ def batch_arm(args) -> None:
                    "total_bf": int(sum(m.number_bf for m in mols)), "waters": int(sizes.sum()),
                    "step": "one batched SCF to convergence (dE, rmsD < 1e-9) of every molecule"},
         "fp64": res["fp64"], "mixed": res["mixed"], "max_abs_dE_mixed_vs_fp64": dE,
-        "setup_s": round(setup_s, 2),
+        "setup_s": round(setup_s, 2), "autotune_s": round(tune_s, 2),
+        "launch_shapes": {f"{c}:{p}": [t, b] for (c, p), (t, b, _) in sorted(tuning.items()) if t},
     }
+    autotune.reset()
     print(json.dumps(line), flush=True)
 
 

@@ -28,6 +28,7 @@ SQ_FP32_BOYS32 = 2
 SQ_OPT_GENERIC_MIN_L = 1
 SQ_OPT_JK_STREAMS = 2
 SQ_OPT_FP64_UNROLLED_HIGH = 3
+SQ_OPT_GRAD_THREAD = 4
 SQ_NOALLOC_MAX_NBF = 1024
 
 PRECISIONS = {"fp64": SQ_FP64, "fp32": SQ_FP32, "fp32_boys32": SQ_FP32_BOYS32}

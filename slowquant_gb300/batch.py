@@ -448,6 +448,32 @@ class BatchSCF:
             self.lists["mixed"] = ([q64, q32], ["fp64", "fp32"])
         self.graphs: dict = {}
         self.builds: list[str] = []
+        self.tuning: dict = {}
+
+    def autotune(self, threads=None, waves=None) -> dict:
+        """Pick each quartet class's launch shape (threads per block, grid cap) for this
+        batch's lists with the project's autotuner, install it, and return the table
+        {(class, precision): (threads, blocks, ms)}.  Call before the first SCF so the
+        captured graphs use the tuned shapes; ``autotune.reset()`` restores the defaults."""
+        from . import autotune
+
+        kw = {}
+        if threads is not None:
+            kw["threads"] = threads
+        if waves is not None:
+            kw["waves"] = waves
+        be = self.be
+
+        def run_class(sub, prec):
+            be.jk_accumulate(self.D, self.Jacc, self.Kacc, self.D32, [sub], [prec])
+
+        table = {}
+        for mode in self.lists:
+            lists, precs = self.lists[mode]
+            table.update(autotune.tune(run_class, lists, precs, **kw))
+        self.tuning = table
+        self.graphs = {}  # re-capture with the tuned shapes
+        return table
 
     def _fock_into_F(self, mode: str) -> None:
         be = self.be

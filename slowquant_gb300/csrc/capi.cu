@@ -85,6 +85,9 @@ static int g_generic_min_l = 5;
 // Bit c set: the FP64 J/K launches of class c run on its kLaunchersF64 kernel,
 // else on the warp kernel (option SQ_OPT_FP64_UNROLLED_HIGH).
 static long long g_fp64_unrolled_high = 0x7FLL << 12;  // classes 12-18
+// Per-thread gradient kernels for the light classes (option SQ_OPT_GRAD_THREAD).
+static int g_grad_thread = 1;
+int grad_thread_enabled() { return g_grad_thread; }
 
 // Autotuned launch shapes per (quartet class, precision); threads 0 = default.
 struct LaunchCfg {
@@ -234,6 +237,10 @@ extern "C" int sq_set_option(int key, long long value) {
         g_jk_streams = (int)value;
         return SQ_OK;
     }
+    if (key == SQ_OPT_GRAD_THREAD) {
+        g_grad_thread = value != 0;
+        return SQ_OK;
+    }
     if (key == SQ_OPT_FP64_UNROLLED_HIGH) {
         if (value < 0 || value >= (1LL << SQ_MAX_QCLASS))
             return set_error(SQ_ERR_ARG, "sq_set_option: class mask out of range");
@@ -261,6 +268,7 @@ extern "C" long long sq_get_option(int key) {
     if (key == SQ_OPT_GENERIC_MIN_L) return g_generic_min_l;
     if (key == SQ_OPT_JK_STREAMS) return g_jk_streams;
     if (key == SQ_OPT_FP64_UNROLLED_HIGH) return g_fp64_unrolled_high;
+    if (key == SQ_OPT_GRAD_THREAD) return g_grad_thread;
     return -1;
 }
 

@@ -12,7 +12,9 @@
 //
 // sq_grad_2e: one warp per quartet forms W'[tuv][cd] (ket transform, |tuv| <= L_ab+1),
 // contracts it with Gamma' and the derivative coefficients of the bra centres,
-// and runs a second time with bra and ket exchanged for the ket centres.
+// and runs a second time with bra and ket exchanged for the ket centres.  The
+// light classes ((ss|ss), (ps|ss), (ps|ps), (pp|ss), (ds|ss)) run the same
+// contraction one quartet per thread (grad_thread.cu).
 // Nothing is stored: each derivative integral is used once and dropped.
 #include "boys.cuh"
 #include "capi_internal.cuh"
@@ -93,6 +95,9 @@ __device__ inline double boys_any(int m, double T, const double *tab) {
     }
     return sum * exp(-T);
 }
+
+cudaError_t launch_grad_thread_class(int qc, const EriArgs &a, int swap, double *grad, cudaStream_t s);
+int grad_thread_enabled();
 
 // Angular momenta of quartet class qc (bra pair class >= ket pair class).
 inline void grad_class_l(int qc, int &la, int &lb, int &lc, int &ld) {
@@ -542,8 +547,13 @@ extern "C" int sq_grad_2e(const sq_basis *basis, const sq_pairs *pairs, const sq
         const size_t sz = (size_t)lay.stride * sizeof(double) * kGradWarps;
         long long blocks = (nq + kGradWarps - 1) / kGradWarps;
         if (blocks > 152LL * 64) blocks = 152LL * 64;
-        for (int swap = 0; swap < 2; ++swap)
+        for (int swap = 0; swap < 2; ++swap) {
+            // light classes: one quartet per thread; the rest: one per warp
+            if (grad_thread_enabled() &&
+                launch_grad_thread_class(c, a, swap, grad, (cudaStream_t)stream) != cudaErrorNotSupported)
+                continue;
             grad2e_kernel<<<(unsigned)blocks, 32 * kGradWarps, sz, (cudaStream_t)stream>>>(a, swap, grad, lay);
+        }
     }
     return check_launch("sq_grad_2e");
 }

@@ -123,3 +123,21 @@ def test_batched_eigh_helper_uniform_stack(gpu_lib):
     W, V = W.cpu().numpy(), V.cpu().numpy()
     np.testing.assert_allclose(W, np.linalg.eigvalsh(M), atol=1e-12)
     np.testing.assert_allclose(M @ V, V * W[:, None, :], atol=1e-11)
+
+
+def test_autotuned_launch_shapes_keep_results(gpu_lib):
+    """The autotuner's launch shapes change timing only: batch energies stay the same."""
+    from slowquant_gb300 import autotune
+    from slowquant_gb300.batch import BatchEngine, BatchSCF
+
+    mols = _mols([2, 1, 3])
+    be = BatchEngine(mols)
+    E0 = BatchSCF(be, "mixed").run()
+    scf = BatchSCF(be, "mixed")
+    try:
+        table = scf.autotune(threads=(64, 128), waves=(1, 8))
+        assert table and all(ms > 0 for _, _, ms in table.values())
+        E1 = scf.run()
+    finally:
+        autotune.reset()
+    np.testing.assert_allclose(E1, E0, atol=1e-9)

@@ -100,3 +100,22 @@ def test_autograd_function_backward(gpu_lib):
     assert abs(float(E) - (-82.94444701585452 + 8.00236706181077)) < 1e-7
     g_ref = gpu_gradient(symbols, xyz.detach().numpy(), "sto-3g")
     np.testing.assert_allclose(xyz.grad.numpy(), g_ref, atol=1e-10)
+
+
+def test_per_thread_gradient_classes_match_warp_kernel(gpu_lib):
+    """The light classes' per-thread gradient kernels == the warp kernel (all classes)."""
+    from slowquant_gb300 import _lib, systems
+    from slowquant_gb300.gradient import rhf_gradient
+    from slowquant_gb300.molecule import _Molecule
+
+    m = _Molecule(systems.water_cluster(2, 5.0, seed=2), 0, "angstrom")
+    m._set_basis_set("cc-pvdz")
+    L = _lib.lib()
+    try:
+        _lib.check(L.sq_set_option(_lib.SQ_OPT_GRAD_THREAD, 0), "sq_set_option")
+        g_warp = rhf_gradient(m, conv=1e-11)
+        _lib.check(L.sq_set_option(_lib.SQ_OPT_GRAD_THREAD, 1), "sq_set_option")
+        g_thread = rhf_gradient(m, conv=1e-11)
+    finally:
+        L.sq_set_option(_lib.SQ_OPT_GRAD_THREAD, 1)
+    np.testing.assert_allclose(g_thread, g_warp, atol=1e-10)
