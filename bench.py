@@ -198,23 +198,26 @@ def max_over_ranks(value: float, world: int, device: str = "cpu") -> float:
 
 
 # ----------------------------------------------------------------- CPU arm
-def cpu_sample(eng_or_none, target_seconds: float, seed: int = 0, pairs_host=None, mol_geom=None):
-    """Time the oracle (faithful restatement of the reference) on random surviving quartets."""
+def cpu_sample(eng_or_none, target_seconds: float, seed: int = 0, pairs_host=None, mol_geom=None, n_fixed=None):
+    """Time the oracle (faithful restatement of the reference) on random surviving quartets.
+
+    Without n_fixed the sample size is calibrated upward until one sample takes
+    about 0.3-1x target_seconds; with n_fixed exactly that many quartets are timed.
+    """
     from oracle import oracle as O
 
     o = O.OracleMolecule(mol_geom, BASIS, "angstrom")
     rng = np.random.default_rng(seed)
     pair_shells, quartets = pairs_host
     nthreads = os.cpu_count() or 1
-    # calibrate on a small sample, then size the timed sample
-    n = 64
+    n = 64 if n_fixed is None else int(n_fixed)
     while True:
         idx = rng.integers(0, len(quartets), n)
         sq = np.concatenate([pair_shells[quartets[idx, 0]], pair_shells[quartets[idx, 1]]], axis=1)
         t0 = time.time()
         o.eri_quartets(sq, nthreads=nthreads, faithful=True)
         dt = time.time() - t0
-        if dt > 0.3 * target_seconds or n >= 2_000_000:
+        if n_fixed is not None or dt > 0.3 * target_seconds or n >= 2_000_000:
             return n / dt, nthreads, n, dt
         n = int(n * min(16.0, max(2.0, 0.5 * target_seconds / max(dt, 1e-3))))
 
@@ -238,9 +241,14 @@ def reference_arm(args) -> None:
     quartets = screening.expand_host(*screening.flatten_tasks(lists[0])[:3], ket)
     rates = []
     t_start = time.time()
+    # calibrate once, then every step times the same number of random quartets
+    # (about cpu_seconds / 2 each, so the whole run stays within a few minutes)
+    rate0, _, n0, dt0 = cpu_sample(None, args.cpu_seconds, seed=12345, pairs_host=(pair_shells, quartets),
+                                   mol_geom=geom)
+    n_step = max(64, int(rate0 * args.cpu_seconds / 2))
     for step in range(args.warmup + args.steps):
         rate, nthreads, n, dt = cpu_sample(None, args.cpu_seconds, seed=step, pairs_host=(pair_shells, quartets),
-                                           mol_geom=geom)
+                                           mol_geom=geom, n_fixed=n_step)
         if step >= args.warmup:
             rates.append(rate)
     value = float(np.median(rates))
@@ -250,7 +258,7 @@ def reference_arm(args) -> None:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config({"total_quartets": len(quartets)}),
         "cpu_baseline": {"value": value, "unit": "quartets/s", "cores": os.cpu_count() or 1, "kind": "port",
-                         "sample": f"per step ~{args.cpu_seconds:.0f} s of uniformly random surviving unique shell "
+                         "sample": f"per step {n_step} (~{args.cpu_seconds / 2:.0f} s) uniformly random surviving unique shell "
                                    f"quartets of the workload through the oracle's faithful C restatement of "
                                    f"electron_repulsion_integral (ms_per_step extrapolates to the full "
                                    f"{len(quartets)}-quartet build)"},
