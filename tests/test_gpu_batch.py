@@ -141,3 +141,11 @@ def test_autotuned_launch_shapes_keep_results(gpu_lib):
     finally:
         autotune.reset()
     np.testing.assert_allclose(E1, E0, atol=1e-9)
+
+
+def test_batch_of_one_molecule(gpu_lib):
+    from slowquant_gb300.batch import BatchEngine, BatchSCF
+
+    mols = _mols([2])
+    E = BatchSCF(BatchEngine(mols), "fp64").run(1e-10, 1e-10)
+    np.testing.assert_allclose(E, [_single_energy(mols[0])], atol=1e-8)

@@ -178,3 +178,35 @@ def test_cauchy_schwarz_inequality_like_reference(gpu_lib):
     np.testing.assert_allclose(_h6_tensor(1e-8), ref, atol=1e-8)
     np.testing.assert_allclose(_h6_tensor(1e-3), ref, atol=1e-3)
     np.testing.assert_allclose(_h6_tensor(1e10), np.zeros(ref.shape), atol=1e-8)
+
+
+def test_edge_cases_small_systems(gpu_lib):
+    """H2 (two basis functions: DIIS passes F through), a lone H atom in UHF, and a
+    J/K build whose screening removes every quartet."""
+    import torch
+
+    from oracle import oracle as O
+
+    # H2 STO-3G RHF against the oracle (nbf = 2 -> the reference's DIIS returns F unchanged)
+    geom = "H 0.0 0.0 0.0;H 1.4 0.0 0.0"
+    A = _run(geom, "sto-3g", "bohr")
+    o = O.OracleMolecule(geom, "sto-3g", "bohr")
+    V = o.eri_dense(1e-12)
+    S, T, Vn = o.one_electron()
+    E_ref = O.run_hartree_fock(S, T, Vn, lambda D: O.jk_from_eri(V, D), o.number_electrons)[0]
+    assert A.molecule.number_bf == 2
+    assert abs(A.hartree_fock.E_hf - E_ref) < 1e-8
+    # a lone H atom: one alpha electron, no beta electrons
+    e = {"geometry": "H 0.0 0.0 0.0;", "unit": "bohr", "basis": "6-31G", "charge": 0, "mix": 0.15}
+    B = _run_uhf(e)
+    o = O.OracleMolecule(e["geometry"], e["basis"], "bohr")
+    V = o.eri_dense(1e-12)
+    S, T, Vn = o.one_electron()
+    E_u = O.run_unrestricted_hartree_fock(S, T, Vn, lambda D: O.jk_from_eri(V, D), 1, 0)[0]
+    assert abs(B.hartree_fock.E_uhf - E_u) < 1e-8
+    np.testing.assert_allclose(B.hartree_fock.rdm1_beta, 0.0, atol=1e-14)
+    # screening that keeps nothing: J = K = 0
+    eng = B.integral.engine
+    D = torch.eye(eng.nbf, dtype=torch.float64, device="cuda")
+    J, K = eng.jk(D, 1e30, "mixed", 1e-4)
+    assert float(J.abs().max()) == 0.0 and float(K.abs().max()) == 0.0
