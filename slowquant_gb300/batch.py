@@ -505,15 +505,21 @@ class BatchSCF:
         self.graphs[mode].replay()
 
     def _eigh_all(self, A_flat: torch.Tensor):
-        """Eigenpairs of every molecule's block of a packed buffer in one launch (sq_batched_eigh)."""
+        """Eigenvectors of every molecule's block of a packed buffer in one launch (sq_batched_eigh).
+
+        The matrices are handed to the kernel largest first: its shared memory
+        is sized by the largest one, so few CTAs fit per SM, and the large
+        matrices should take the first wave with the small ones behind them."""
         be = self.be
         if not hasattr(self, "_eig_desc"):
             dev = be.device
             nbf = np.array(be.mol_nbf, dtype=np.int64)
-            self._eig_desc = (torch.tensor(np.array(be.mol_base, dtype=np.int64), device=dev),
-                              torch.tensor(nbf.astype(np.int32), device=dev),
-                              torch.tensor(np.concatenate([[0], np.cumsum(nbf)[:-1]]).astype(np.int64), device=dev),
-                              int(nbf.sum()), int(nbf.max()))
+            base = np.array(be.mol_base, dtype=np.int64)
+            woff = np.concatenate([[0], np.cumsum(nbf)[:-1]]).astype(np.int64)
+            order = np.argsort(-nbf, kind="stable")
+            self._eig_desc = (torch.tensor(base[order], device=dev),
+                              torch.tensor(nbf[order].astype(np.int32), device=dev),
+                              torch.tensor(woff[order], device=dev), int(nbf.sum()), int(nbf.max()))
         offs, dims, woffs, ntot, nmax = self._eig_desc
         if nmax > _EIGH_MAX_N:
             out = torch.empty_like(A_flat)

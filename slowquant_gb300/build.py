@@ -64,8 +64,17 @@ def build(jobs: int | None = None, force: bool = False, verbose: bool = False, e
         if force or not os.path.exists(o) or os.path.getmtime(o) < max(os.path.getmtime(s), hdr):
             todo.append((s, o))
     jobs = jobs or max(1, os.cpu_count() or 1)
-    # longest translation units first
-    todo.sort(key=lambda so: -os.path.getsize(so[0]))
+    # longest translation units first: the per-class kernels of the high classes
+    # (eri_q12..q18 and their FP64 variants) take 1-2 minutes each, the rest seconds
+    def cost(so):
+        base = os.path.basename(so[0])[:-3]
+        if base.startswith("eri_q"):
+            num = base[5:].split("_")[0]
+            if num.isdigit():
+                return 100 * int(num) + (50 if base.endswith("_f64") else 0)
+        return os.path.getsize(so[0]) / 1e4
+
+    todo.sort(key=lambda so: -cost(so))
     if todo:
         with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
             futs = [ex.submit(_compile, s, o, extra) for s, o in todo]
