@@ -159,7 +159,9 @@ const char *sq_last_error(void);
  * into the caller's stream with events, so that one class's tail overlaps the
  * next class; 1 launches everything on the caller's stream.  Successive calls
  * take the next streams of a pool of 16, so calls issued concurrently from
- * different caller streams run side by side. */
+ * different caller streams run side by side.  The pool (streams and events,
+ * kept until the process exits) is created by the first multi-stream J/K call
+ * on each device: make that call outside any stream capture. */
 #define SQ_OPT_JK_STREAMS 2
 /* SQ_OPT_FP64_UNROLLED_HIGH: bit mask over quartet classes; a set bit runs
  * that class's FP64 J/K launches on its per-thread kernel where one exists
