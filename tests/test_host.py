@@ -169,3 +169,51 @@ def test_sub_slot_table_partitions_each_slot():
             np.testing.assert_array_equal(t["hbase"][ids], hbase[s] + lo * E[s] * pstride[s])
             np.testing.assert_allclose(t["qsum"][ids].sum(), q[off[s]:off[s] + npp[s]].sum(), rtol=1e-12)
             assert npp[s] >= S
+
+
+def test_ket_chunk_partition():
+    """_ket_chunks: every (bra, ket) entry is kept whole or cut into all of its ket
+    chunks, and each piece lands in FP64 exactly when its bound reaches tau."""
+    from types import SimpleNamespace
+
+    import numpy as np
+
+    from slowquant_gb300 import screening
+    from slowquant_gb300.engine import IntegralEngine
+
+    rng = np.random.default_rng(5)
+    nslot = 30
+    npp = rng.integers(1, 40, nslot)
+    pstride = np.ones(nslot, np.int64)
+    pbase = np.concatenate([[0], np.cumsum(npp)[:-1]])
+    E = np.ones(nslot, np.int64)
+    q = np.sort(rng.uniform(0, 0.2, int(npp.sum())))[::-1]
+    qcum = np.concatenate([[0.0], np.cumsum(q)])
+    first, t = screening.sub_slot_table(npp, pbase, pstride, pbase, E, np.ones(nslot), qcum, pbase,
+                                        int(npp.max()), 512, 2)
+    qs = np.concatenate([qcum[pbase + npp] - qcum[pbase], t["qsum"]])
+    fake = SimpleNamespace(slot_qsum=qs, slot_npp=np.concatenate([npp, t["npp"]]), sub_first=first)
+    fake._ket_chunks = IntegralEngine._ket_chunks.__get__(fake)
+    entries = np.stack([rng.integers(0, nslot, 400), rng.integers(0, nslot, 400)], 1).astype(np.int32)
+    tau = 0.05
+    e64, e32 = fake._ket_chunks(entries, tau)
+    # bounds on the right side of tau: FP64 pieces reach it; an FP32 piece is below it,
+    # or is a whole ket each of whose chunks is below it (same arithmetic as its chunks)
+    assert np.all(qs[e64[:, 0]] * qs[e64[:, 1]] >= tau)
+    for b, k in e32:
+        if qs[b] * qs[k] < tau:
+            continue
+        assert k < nslot
+        S = max(S for S in first if first[S][k] >= 0 and npp[k] >= 4 * S)
+        chunks = first[S][k] + np.arange(S)
+        assert np.all(qs[b] * qs[chunks] < tau)
+    # every entry's ket primitive pairs are covered exactly once
+    npp_all = fake.slot_npp
+    got = {}
+    for b, k in np.concatenate([e64, e32]):
+        parent = k if k < nslot else t["parent"][k - nslot]
+        got[(b, parent)] = got.get((b, parent), 0) + int(npp_all[k])
+    want = {}
+    for b, k in entries:
+        want[(b, k)] = want.get((b, k), 0) + int(npp[k])
+    assert got == want
