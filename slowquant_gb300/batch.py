@@ -263,10 +263,15 @@ class BatchEngine:
     def quartets(self, threshold: float, fp32_threshold: float | None = None):
         """Screened unique quartets of every molecule (slot ids), one segment per class,
         tasks of all molecules merged heaviest first."""
-        key = (threshold, fp32_threshold)
+        mask_now = int(self.lib.sq_get_option(_lib.SQ_OPT_FP64_UNROLLED_HIGH))
+        key = (threshold, fp32_threshold, mask_now)
         if key in self._lists:
             return self._lists[key]
         nl = 1 if fp32_threshold is None else 2
+        # FP64 classes 12-18 split only while all of them run on per-thread kernels
+        mask = int(self.lib.sq_get_option(_lib.SQ_OPT_FP64_UNROLLED_HIGH))
+        hi = 18 if all((mask >> c) & 1 for c in range(12, 19)) else 11
+        split_max = [hi, hi]
         merged = [{c: [] for c in range(screening.NQCLASS)} for _ in range(nl)]
         for mi in range(self.nmol):
             sel = np.nonzero(self.pair_mol == mi)[0]
@@ -282,7 +287,7 @@ class BatchEngine:
                         bslots = self.slot_of_pair[sel[bra]]
                         # heavy quartets of the per-thread classes: bra sub-slot chunks
                         S = 1
-                        if c <= (11 if li == 0 else 18):
+                        if c <= split_max[li]:
                             while cost * CLASS_WEIGHT[c] > SPLIT_TARGET * S and (2 * S) in self.sub_first and \
                                     self.sub_first[2 * S][bslots[0]] >= 0:
                                 S *= 2
@@ -416,7 +421,8 @@ class _BatchDIIS:
         B[:, :m, :m] = Bm
         b0 = torch.zeros((count, m + 1), dtype=torch.float64, device=F.device)
         b0[:, -1] = -1
-        c = torch.linalg.solve(B, b0)
+        # solve_ex: no singularity check, so no host synchronisation per group
+        c = torch.linalg.solve_ex(B, b0)[0]
         return torch.einsum("ci,icpq->cpq", c[:, :m], Fs)
 
 

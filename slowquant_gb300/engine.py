@@ -474,8 +474,9 @@ class IntegralEngine:
         is applied per bra chunk of the FP64 quartets of the per-thread classes:
         a chunk goes to FP32 when the sum of its primitive Schwarz factors times
         the ket's is below fp32_threshold."""
+        hi = self._fp64_per_thread_max()
         key = (float(threshold), None if fp32_threshold is None else float(fp32_threshold), bool(split),
-               bool(chunks))
+               bool(chunks), hi)
         if q is None and key in self._quartet_cache:
             return self._quartet_cache[key]
         self._require_eri()
@@ -485,10 +486,10 @@ class IntegralEngine:
         lists, ket_list = screening.build_tasks(self.pair_class, npp_eff, np.ones_like(npp_eff), qv, threshold,
                                                 fp32_threshold)
         self.slots  # canonical slot numbering (from the engine's own Schwarz factors)
-        # classes with per-thread kernels: 0-11 in FP64, 0-18 in FP32
-        split_max = [11, 18] if split else [-1, -1]
+        # classes with per-thread kernels: 0-18 (FP64: 12-18 unless switched off) and FP32 0-18
+        split_max = [hi, 18] if split else [-1, -1]
         if chunks and fp32_threshold is not None:
-            out = self._chunk_lists(lists, ket_list, float(fp32_threshold))
+            out = self._chunk_lists(lists, ket_list, float(fp32_threshold), hi)
         else:
             out = [self._expand(t, ket_list, split_max[li]) for li, t in enumerate(lists)]
         res = out[0] if len(out) == 1 else (out[0], out[1])
@@ -496,17 +497,25 @@ class IntegralEngine:
             self._quartet_cache[key] = res
         return res
 
-    def _chunk_lists(self, lists, ket_list: np.ndarray, tau: float):
+    def _fp64_per_thread_max(self) -> int:
+        """Highest class index up to which every FP64 J/K launch runs on a per-thread kernel
+        (18 with the default SQ_OPT_FP64_UNROLLED_HIGH, 11 otherwise).  Sub-slot chunks
+        of one quartet must all go through kernels of the same kind, which number a
+        slot's primitive pairs the same way."""
+        mask = int(self.lib.sq_get_option(_lib.SQ_OPT_FP64_UNROLLED_HIGH))
+        return 18 if all((mask >> c) & 1 for c in range(12, 19)) else 11
+
+    def _chunk_lists(self, lists, ket_list: np.ndarray, tau: float, hi: int = 18):
         """(FP64, FP32) lists with the precision test per bra primitive chunk.
 
-        FP64 quartets of the per-thread classes (0-11) are cut into S chunks of
+        FP64 quartets of the per-thread classes (0-18) are cut into S chunks of
         their bra's primitive pairs (sorted by descending factor, CHUNK_MIN to
         2 CHUNK_MIN per chunk, more when the quartet is heavy), kets are cut the same way where
         a ket straddles the threshold, and each (bra chunk, ket chunk) is placed
         by its own bound; FP32 quartets stay whole.
         """
         t64, t32 = lists
-        q32 = self._expand(t32, ket_list, 18)
+        q32 = self._expand(t32, ket_list, hi)
         npp = self.slot_npp
         ket_slots = self.slot_of_pair[ket_list]
         keep64 = {c: [] for c in range(screening.NQCLASS)}
@@ -515,7 +524,7 @@ class IntegralEngine:
         for c in range(screening.NQCLASS):
             for m, st, n in t64[c]:
                 slots = self.slot_of_pair[m]
-                if c > 11 or len(m) == 0:
+                if c > hi or len(m) == 0:
                     whole64[c].append((m, st, n))  # pair ids: _expand maps them to slots
                     continue
                 nb = int(npp[slots[0]])

@@ -277,8 +277,8 @@ def test_chunk_level_mixed_precision():
     c64, c32 = eng.quartets(1e-12, 1e-4, chunks=True)
     assert prims(c64) < prims(q64)
     assert prims(c64) + prims(c32) == prims(q64) + prims(q32)  # same primitive quartets, re-partitioned
-    # every chunk kept in FP64 (per-thread classes 0-11) has a large bound
-    p = c64.pairs[: int(c64.class_off[12])].cpu().numpy()
+    # every chunk kept in FP64 (per-thread classes 0-18) has a large bound
+    p = c64.pairs[: int(c64.class_off[19])].cpu().numpy()
     assert np.all(eng.slot_qsum[p[:, 0]] * eng.slot_qsum[p[:, 1]] >= 1e-4)
     assert np.max(np.abs(Jm - J0)) < 1e-6
 
