@@ -169,8 +169,8 @@ const char *sq_last_error(void);
  * kernel.  Default: classes 12-18. */
 #define SQ_OPT_FP64_UNROLLED_HIGH 3
 /* SQ_OPT_GRAD_THREAD: 1 (default) runs the gradient of the light classes
- * ((ss|ss), (ps|ss), (ps|ps), (pp|ss), (ds|ss)) one quartet per thread,
- * 0 one quartet per warp like the other classes. */
+ * ((ss|ss), (ps|ss), (ps|ps), (pp|ss), (pp|ps), (ds|ss), (ds|ps), (dp|ss))
+ * one quartet per thread, 0 one quartet per warp like the other classes. */
 #define SQ_OPT_GRAD_THREAD 4
 int sq_set_option(int key, long long value);
 long long sq_get_option(int key);

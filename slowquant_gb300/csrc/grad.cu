@@ -13,8 +13,9 @@
 // sq_grad_2e: one warp per quartet forms W'[tuv][cd] (ket transform, |tuv| <= L_ab+1),
 // contracts it with Gamma' and the derivative coefficients of the bra centres,
 // and runs a second time with bra and ket exchanged for the ket centres.  The
-// light classes ((ss|ss), (ps|ss), (ps|ps), (pp|ss), (ds|ss)) run the same
-// contraction one quartet per thread (grad_thread.cu).
+// light classes ((ss|ss), (ps|ss), (ps|ps), (pp|ss), (pp|ps), (ds|ss),
+// (ds|ps), (dp|ss)) run the same contraction one quartet per thread
+// (grad_thread.cu).
 // Nothing is stored: each derivative integral is used once and dropped.
 #include "boys.cuh"
 #include "capi_internal.cuh"

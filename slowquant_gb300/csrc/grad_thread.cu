@@ -240,8 +240,14 @@ cudaError_t launch_grad_thread_class(int qc, const EriArgs &a, int swap, double 
         case 2 * 2 + 1: return launch_grad_thread<1, 0, 1, 0>(a, swap, grad, s);  // (ps|ps)
         case 3 * 2 + 0: return launch_grad_thread<1, 1, 0, 0>(a, swap, grad, s);  // (pp|ss)
         case 3 * 2 + 1: return launch_grad_thread<0, 0, 1, 1>(a, swap, grad, s);
+        case 4 * 2 + 0: return launch_grad_thread<1, 1, 1, 0>(a, swap, grad, s);  // (pp|ps)
+        case 4 * 2 + 1: return launch_grad_thread<1, 0, 1, 1>(a, swap, grad, s);
         case 6 * 2 + 0: return launch_grad_thread<2, 0, 0, 0>(a, swap, grad, s);  // (ds|ss)
         case 6 * 2 + 1: return launch_grad_thread<0, 0, 2, 0>(a, swap, grad, s);
+        case 7 * 2 + 0: return launch_grad_thread<2, 0, 1, 0>(a, swap, grad, s);  // (ds|ps)
+        case 7 * 2 + 1: return launch_grad_thread<1, 0, 2, 0>(a, swap, grad, s);
+        case 10 * 2 + 0: return launch_grad_thread<2, 1, 0, 0>(a, swap, grad, s);  // (dp|ss)
+        case 10 * 2 + 1: return launch_grad_thread<0, 0, 2, 1>(a, swap, grad, s);
         default: return cudaErrorNotSupported;
     }
 }
