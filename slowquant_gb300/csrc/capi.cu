@@ -178,10 +178,10 @@ static cudaError_t launch_class(EriArgs &args, const sq_quartets *qs, int c, int
 }
 
 static int run_classes(const char *who, EriArgs args, const sq_quartets *qs, int mode, int precision,
-                       cudaStream_t stream) {
+                       cudaStream_t stream, bool pooled = true) {
     int nonempty = 0;
     for (int c = 0; c < SQ_MAX_QCLASS; ++c) nonempty += qs->class_off[c + 1] > qs->class_off[c];
-    const int nstream = g_jk_streams < nonempty ? g_jk_streams : nonempty;
+    const int nstream = !pooled ? 1 : (g_jk_streams < nonempty ? g_jk_streams : nonempty);
     if (mode == MODE_JK && nstream > 1) {
         std::lock_guard<std::mutex> lock(g_pool_mutex);
         StreamPool *pool = nullptr;
@@ -304,7 +304,8 @@ extern "C" int sq_eri_dense(const sq_basis *basis, const sq_pairs *pairs, const 
 
 static int jk_common(const char *who, const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots,
                      const sq_quartets *quartets, const double *table64, const float *table32, int nd,
-                     const double *D, float *D32, double *Jacc, double *Kacc, int precision, void *stream) {
+                     const double *D, float *D32, double *Jacc, double *Kacc, int precision, void *stream,
+                     bool pooled = true) {
     int rc = check_common(who, basis, pairs, quartets, table64);
     if (rc) return rc;
     if (!slots || !slots->prim || !slots->herm || !slots->pair)
@@ -334,7 +335,16 @@ static int jk_common(const char *who, const sq_basis *basis, const sq_pairs *pai
     a.use_slots = 1;
     a.Jacc = Jacc;
     a.Kacc = Kacc;
-    return run_classes(who, a, quartets, MODE_JK, precision, s);
+    return run_classes(who, a, quartets, MODE_JK, precision, s, pooled);
+}
+
+// sq_jk with every class launch on the caller's stream: no library streams or
+// events are created (the allocation-free entry point uses it).
+int sq::jk_serial(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, const sq_quartets *quartets,
+              const double *table64, const float *table32, const double *D, float *D32, double *Jacc, double *Kacc,
+              int precision, void *stream) {
+    return jk_common("sq_jk_noalloc", basis, pairs, slots, quartets, table64, table32, 1, D, D32, Jacc, Kacc,
+                     precision, stream, false);
 }
 
 extern "C" int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots,

@@ -71,5 +71,7 @@ extern "C" int sq_jk_noalloc(const sq_basis *basis, const sq_pairs *pairs, const
         const int rc = scratch_address(&d32);
         if (rc != SQ_OK) return rc;
     }
-    return sq_jk(basis, pairs, slots, quartets, table64, table32, D, d32, Jacc, Kacc, precision, stream);
+    // serial launches on the caller's stream: the library's stream pool would
+    // create streams and events on its first use
+    return sq::jk_serial(basis, pairs, slots, quartets, table64, table32, D, d32, Jacc, Kacc, precision, stream);
 }
