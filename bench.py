@@ -143,7 +143,7 @@ def class_work(eng, ql, precision: str = "fp64") -> dict:
     """
     import torch
 
-    from slowquant_gb300 import flops
+    from slowquant_gb300 import _lib, flops
 
     # quartet entries are slot ids: primitive pairs per slot
     npp_slot = torch.tensor(eng.slot_npp, dtype=torch.int64, device=eng.device)
@@ -154,7 +154,7 @@ def class_work(eng, ql, precision: str = "fp64") -> dict:
     kk = sub >> 16
     npp_all = (npp_all * (kk + 1)) // S - (npp_all * kk) // S
     out = {}
-    for c in range(21):
+    for c in range(_lib.SQ_MAX_QCLASS):
         a, b = int(ql.class_off[c]), int(ql.class_off[c + 1])
         if b == a:
             continue
@@ -443,8 +443,8 @@ def gpu_arm(args) -> None:
     peak = peak64 if dom["precision"] == "fp64" else peak32
     achieved = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
     fl64 = sum(w["flops"] for w in work_all.values())
-    launches = sum(1 for c in range(21) if q64.class_off[c + 1] > q64.class_off[c]) + sum(
-        1 for c in range(21) if q32.class_off[c + 1] > q32.class_off[c]) + 2
+    launches = sum(1 for c in range(_lib.SQ_MAX_QCLASS) if q64.class_off[c + 1] > q64.class_off[c]) + sum(
+        1 for c in range(_lib.SQ_MAX_QCLASS) if q32.class_off[c + 1] > q32.class_off[c]) + 2
 
     clocks = clk.summary()
     line = {

@@ -27,14 +27,19 @@ extern "C" {
 #define SQ_ERR_CUDA 3         /* CUDA launch or runtime error */
 #define SQ_ERR_NONFINITE 4    /* NaN or Inf found in an output */
 
-#define SQ_MAX_L 2            /* highest shell angular momentum (d) of the ERI kernels */
-#define SQ_MAX_QCLASS 21      /* quartet classes for l <= SQ_MAX_L: 6 pair classes -> 21 */
+#define SQ_MAX_L 3            /* highest shell angular momentum (f) of the ERI / J-K kernels */
+#define SQ_MAX_QCLASS 55      /* quartet classes for l <= SQ_MAX_L: 10 pair classes -> 55;
+                                 classes 0-20 hold s, p, d shells only */
+#define SQ_MAX_L_GRAD 2       /* highest shell angular momentum of the gradient kernels */
 
 /* Boys-function grid, T_k = k / SQ_BOYS_STEP_INV, k < SQ_BOYS_NGRID.
  * FP64 table (SQ_BOYS_TAB64_SIZE doubles):
  *   [0, NGRID*NCOL): F_m(T_k) at [k*NCOL + m], m < NCOL-1; column NCOL-1 = exp(-T_k);
  *   [SQ_BOYS_TAY64_OFF, ...): Taylor coefficients F_{m+j}(T_k)/j! at
  *     [(m*NGRID + k)*8 + j], j < 7, m < 15; block m = 15 holds exp(-T_k)/j!.
+ *   [SQ_BOYS_HI64_OFF, ...): high-order grid for the classes with f shells,
+ *     F_m(T_k) at [k*HI_NCOL + m], m < HI_NCOL-1, k < SQ_BOYS_HI_NGRID; column
+ *     HI_NCOL-1 = exp(-T_k).  Same step; tabulated to SQ_BOYS_HI_TMAX.
  * FP32 table (SQ_BOYS_TAB32_SIZE floats): the same F grid, then
  *   [SQ_BOYS_TAY32_OFF + (m*NGRID + k)*4 + j], j < 4. */
 #define SQ_BOYS_NGRID 580
@@ -42,7 +47,11 @@ extern "C" {
 #define SQ_BOYS_NCOL 16
 #define SQ_BOYS_TMAX 36.0
 #define SQ_BOYS_TAY64_OFF (SQ_BOYS_NGRID * SQ_BOYS_NCOL)
-#define SQ_BOYS_TAB64_SIZE (SQ_BOYS_TAY64_OFF + 16 * SQ_BOYS_NGRID * 8)
+#define SQ_BOYS_HI_NGRID 968
+#define SQ_BOYS_HI_NCOL 24
+#define SQ_BOYS_HI_TMAX 60.0
+#define SQ_BOYS_HI64_OFF (SQ_BOYS_TAY64_OFF + 16 * SQ_BOYS_NGRID * 8)
+#define SQ_BOYS_TAB64_SIZE (SQ_BOYS_HI64_OFF + SQ_BOYS_HI_NGRID * SQ_BOYS_HI_NCOL)
 #define SQ_BOYS_TAY32_OFF (SQ_BOYS_NGRID * SQ_BOYS_NCOL)
 #define SQ_BOYS_TAB32_SIZE (SQ_BOYS_TAY32_OFF + 16 * SQ_BOYS_NGRID * 4)
 
@@ -189,10 +198,12 @@ int sq_set_launch_config(int qclass, int precision, int threads, long long max_b
  * (slowquant/molecularintegrals/integralfunctions.py:74-97). */
 int sq_boys_table(double *table64, float *table32, void *stream);
 
-/* F_0..F_{n_max}(z[i]) for nz arguments -> out[nz][n_max+1]; n_max <= 8.
- * mode 0: the tabulated function the J/K kernels use; mode 1: the reference's
- * piecewise formula that the dense-tensor and Schwarz kernels use.  Test hook
- * for boys_function (integralfunctions.py:74-97). */
+/* F_0..F_{n_max}(z[i]) for nz arguments -> out[nz][n_max+1].
+ * mode 0: the tabulated function the J/K kernels of classes 0-20 use (n_max <= 8);
+ * mode 1: the reference's piecewise formula that the dense-tensor and Schwarz
+ * kernels use (n_max <= 22); mode 2: the high-order table of the J/K kernels of
+ * the classes with f shells (n_max <= 16).  Test hook for boys_function
+ * (integralfunctions.py:74-97). */
 int sq_boys(int n_max, const double *z, long long nz, const double *table64, int mode, double *out, void *stream);
 
 /* Primitive-pair data for every pair in `pairs`: P, p, U and the Hermite

@@ -71,7 +71,7 @@ void sqo_set_boys_mode(int mode) { g_boys_mode = mode; }
 
 static double boys_exact(int n, double z) {
     const double pi = 3.141592653589793;
-    if (z > 40.0) {
+    if (z > 60.0) {
         double F = 0.5 * sqrt(pi / z);
         for (int m = 0; m < n; m++) F *= (2 * m + 1) / (2.0 * z);
         return F;
@@ -209,13 +209,22 @@ static int shell_lmax(const sqo_basis *B, int s) {
  * contracted block [nbf1][nbf2][nbf3][nbf4].  work must hold eri_work_size()
  * doubles.
  */
-static size_t eri_work_size(int maxL, int maxprim, int maxcart) {
+static size_t eri_work_size(const sqo_basis *B) {
+    int maxL = 0, maxprim = 0;
+    size_t maxcp = 0; /* largest (components x primitives) of one shell */
+    for (int s = 0; s < B->nshell; s++) {
+        const int l = shell_lmax(B, s);
+        if (l > maxL) maxL = l;
+        if (B->nprim[s] > maxprim) maxprim = B->nprim[s];
+        const size_t cp = (size_t)B->ncart[s] * B->nprim[s];
+        if (cp > maxcp) maxcp = cp;
+    }
     size_t Lt = 4 * (size_t)maxL;
     size_t rtab = (Lt + 1) * (Lt + 1) * (Lt + 1) * (3 * Lt + 2);
     size_t rout = (Lt + 1) * (Lt + 1) * (Lt + 1);
     size_t e1 = (size_t)(maxL + 1) * (maxL + 1) * (2 * maxL + 1);
     size_t pre = (size_t)maxprim * maxprim * e1 * 3;
-    size_t vprim = (size_t)maxcart * maxcart * maxcart * maxcart * maxprim * maxprim * maxprim * maxprim;
+    size_t vprim = maxcp * maxcp * maxcp * maxcp;
     return rtab + rout + 3 * e1 + pre + vprim;
 }
 
@@ -357,7 +366,7 @@ static void basis_limits(const sqo_basis *B, int *maxL, int *maxprim, int *maxca
 int sqo_eri_block(const sqo_basis *B, int s1, int s2, int s3, int s4, double *out, int faithful) {
     int maxL, maxprim, maxcart;
     basis_limits(B, &maxL, &maxprim, &maxcart);
-    double *work = (double *)malloc(eri_work_size(maxL, maxprim, maxcart) * sizeof(double));
+    double *work = (double *)malloc(eri_work_size(B) * sizeof(double));
     if (!work) return 1;
     eri_block(B, s1, s2, s3, s4, out, work, faithful);
     free(work);
@@ -369,7 +378,7 @@ int sqo_schwarz(const sqo_basis *B, double *cs, int nthreads, int faithful) {
     int maxL, maxprim, maxcart;
     basis_limits(B, &maxL, &maxprim, &maxcart);
     const int n = B->nshell;
-    const size_t wsz = eri_work_size(maxL, maxprim, maxcart);
+    const size_t wsz = eri_work_size(B);
     const size_t bsz = (size_t)maxcart * maxcart * maxcart * maxcart;
     int err = 0;
 #ifdef _OPENMP
@@ -413,7 +422,7 @@ int sqo_eri_dense(const sqo_basis *B, const double *cs, double thr, double *V, i
     basis_limits(B, &maxL, &maxprim, &maxcart);
     const int n = B->nshell;
     const size_t nbf = (size_t)B->nbf;
-    const size_t wsz = eri_work_size(maxL, maxprim, maxcart);
+    const size_t wsz = eri_work_size(B);
     const size_t bsz = (size_t)maxcart * maxcart * maxcart * maxcart;
     memset(V, 0, nbf * nbf * nbf * nbf * sizeof(double));
     int err = 0;
@@ -476,7 +485,7 @@ int sqo_eri_quartets(const sqo_basis *B, const int *quartets, long nq, double *o
                      int nthreads, int faithful) {
     int maxL, maxprim, maxcart;
     basis_limits(B, &maxL, &maxprim, &maxcart);
-    const size_t wsz = eri_work_size(maxL, maxprim, maxcart);
+    const size_t wsz = eri_work_size(B);
     int err = 0;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);

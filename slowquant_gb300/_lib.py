@@ -14,13 +14,22 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libsqgb300.so")
 
 SQ_OK = 0
-SQ_MAX_L = 2
-SQ_MAX_QCLASS = 21
+SQ_ERR_ARG = 1
+SQ_ERR_UNSUPPORTED = 2
+SQ_ERR_CUDA = 3
+SQ_ERR_NONFINITE = 4
+SQ_MAX_L = 3
+SQ_MAX_QCLASS = 55
+SQ_MAX_L_GRAD = 2
 SQ_BOYS_NGRID = 580
 SQ_BOYS_STEP_INV = 16
 SQ_BOYS_NCOL = 16
 SQ_BOYS_TMAX = 36.0
-SQ_BOYS_TAB64_SIZE = SQ_BOYS_NGRID * SQ_BOYS_NCOL + 16 * SQ_BOYS_NGRID * 8
+SQ_BOYS_HI_NGRID = 968
+SQ_BOYS_HI_NCOL = 24
+SQ_BOYS_HI_TMAX = 60.0
+SQ_BOYS_HI64_OFF = SQ_BOYS_NGRID * SQ_BOYS_NCOL + 16 * SQ_BOYS_NGRID * 8
+SQ_BOYS_TAB64_SIZE = SQ_BOYS_HI64_OFF + SQ_BOYS_HI_NGRID * SQ_BOYS_HI_NCOL
 SQ_BOYS_TAB32_SIZE = SQ_BOYS_NGRID * SQ_BOYS_NCOL + 16 * SQ_BOYS_NGRID * 4
 SQ_FP64 = 0
 SQ_FP32 = 1

@@ -85,7 +85,7 @@ class BatchEngine:
         self.mat_total = base
         self.l = np.array(l, dtype=np.int32)
         if self.l.max() > _lib.SQ_MAX_L:
-            raise NotImplementedError("batched ERI kernels support shells up to d")
+            raise NotImplementedError(f"ERI kernels support shells up to l={_lib.SQ_MAX_L}")
         self.nprim = np.array(nprim, dtype=np.int32)
         self.shell_mol = np.array(shell_mol, dtype=np.int32)
         prim_off = np.concatenate([[0], np.cumsum(self.nprim)[:-1]]).astype(np.int32)

@@ -179,6 +179,28 @@ __device__ inline void boys64_rt(int m_max, double T, const double *__restrict__
     }
 }
 
+// High-order FP64 Boys F_m(T), m <= 16, from the grid at SQ_BOYS_HI64_OFF
+// (the classes with f shells reach m = 12): the same 7-term Taylor expansion
+// about the nearest grid point, each order on its own; beyond
+// SQ_BOYS_HI_TMAX (60) the asymptote F_m = sqrt(pi/T)/2 prod_{j<m} (2j+1)/(2T),
+// whose neglected term is below 2e-13 relative for m <= 13 there.
+__device__ __forceinline__ double boys_hi(int m, double T, const double *__restrict__ tab64) {
+    if (T < SQ_BOYS_HI_TMAX) {
+        const int k = __double2int_rn(T * SQ_BOYS_STEP_INV);
+        const double d = T - k * (1.0 / SQ_BOYS_STEP_INV);
+        const double *row = tab64 + SQ_BOYS_HI64_OFF + k * SQ_BOYS_HI_NCOL + m;
+        double f = __ldg(row + kBoysTaylor64 - 1);
+#pragma unroll
+        for (int j = kBoysTaylor64 - 1; j >= 1; --j) f = fma(f, -d * (1.0 / j), __ldg(row + j - 1));
+        return f;
+    }
+    const double r = rsqrt(T);
+    double f = kSqrtPiHalf * r;
+    const double h = 0.5 * r * r;
+    for (int j = 0; j < m; ++j) f *= (2 * j + 1) * h;
+    return f;
+}
+
 // Reference-compatible Boys function: the piecewise formula of
 // slowquant/molecularintegrals/integralfunctions.py:74-97 restated term for
 // term (erf form for n = 0, large-z asymptote for z > 25, zero-z limit, and

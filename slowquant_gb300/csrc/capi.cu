@@ -40,6 +40,9 @@ static const eri_launcher kLaunchersF32[SQ_MAX_QCLASS] = {
     launch_qc_14_f32, launch_qc_15_f32, launch_qc_16_f32, launch_qc_17_f32, launch_qc_18_f32, nullptr, nullptr,
 };
 
+// Classes with an f shell (eri_block.cu): one CTA per contracted quartet.
+cudaError_t launch_eri_block(const EriArgs &, int, int, int, int, int, int, cudaStream_t);
+
 #define DECL64(QC) cudaError_t launch_qc_##QC##_f64(const EriArgs &, int, int, cudaStream_t);
 DECL64(12) DECL64(13) DECL64(14) DECL64(15) DECL64(16) DECL64(17) DECL64(18)
 #undef DECL64
@@ -56,8 +59,9 @@ static const eri_launcher kLaunchersF64[SQ_MAX_QCLASS] = {
 
 // Per-thread (fully unrolled) J/K kernels exist for the light classes (L <= 4,
 // except (dd|ss)) in every precision, and for classes 12-18 in SQ_FP64 and
-// SQ_FP32; every other class/precision, and every dense-tensor or Schwarz
-// launch, runs on the generic warp kernel.
+// SQ_FP32; every other class/precision of s, p and d shells, and every
+// dense-tensor or Schwarz launch of those, runs on the generic warp kernel.
+// Classes 21-54 (with an f shell) always run on the block kernel.
 // SQ_OPT_GENERIC_MIN_L = 0 sends everything to it.
 static const eri_launcher kLaunchers[SQ_MAX_QCLASS] = {
     launch_qc_0, launch_qc_1, launch_qc_2, launch_qc_3, launch_qc_4, launch_qc_5, launch_qc_6,
@@ -165,6 +169,8 @@ static cudaError_t launch_class(EriArgs &args, const sq_quartets *qs, int c, int
         args.cfg_threads = 0;
         args.cfg_blocks = 0;
     }
+    if (la > SQ_LMAX || lb > SQ_LMAX || lc > SQ_LMAX || ld > SQ_LMAX)
+        return launch_eri_block(args, la, lb, lc, ld, mode, precision, stream);
     const int L = la + lb + lc + ld;
     eri_launcher unrolled = nullptr;
     if (mode == MODE_JK && L < g_generic_min_l) unrolled = kLaunchers[c];

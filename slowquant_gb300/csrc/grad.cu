@@ -17,6 +17,8 @@
 // (ds|ps), (dp|ss)) run the same contraction one quartet per thread
 // (grad_thread.cu).
 // Nothing is stored: each derivative integral is used once and dropped.
+#include <cstdlib>
+
 #include "boys.cuh"
 #include "capi_internal.cuh"
 #include "eri.cuh"
@@ -524,6 +526,14 @@ extern "C" int sq_grad_2e(const sq_basis *basis, const sq_pairs *pairs, const sq
         return set_error(SQ_ERR_ARG, "sq_grad_2e: NULL argument");
     if (basis->mat_base) return set_error(SQ_ERR_ARG, "sq_grad_2e: batched (packed) bases are not supported");
     if (quartets->nquartet == 0) return SQ_OK;
+    for (int c = 0; c < SQ_MAX_QCLASS; ++c) {
+        if (quartets->class_off[c + 1] <= quartets->class_off[c]) continue;
+        int la, lb, lc, ld;
+        grad_class_l(c, la, lb, lc, ld);
+        if (la > SQ_MAX_L_GRAD || lb > SQ_MAX_L_GRAD || lc > SQ_MAX_L_GRAD || ld > SQ_MAX_L_GRAD)
+            return set_error(SQ_ERR_UNSUPPORTED, "sq_grad_2e: class %d has l > %d (no gradient kernel)", c,
+                             SQ_MAX_L_GRAD);
+    }
     EriArgs a{};
     a.basis = *basis;
     a.pairs = *pairs;
@@ -566,6 +576,21 @@ extern "C" int sq_grad_1e(const sq_basis *basis, const double *table64, const do
     if (basis->mat_base) return set_error(SQ_ERR_ARG, "sq_grad_1e: batched (packed) bases are not supported");
     const int np = basis->nshell * (basis->nshell + 1) / 2;
     if (np == 0) return SQ_OK;
+    {
+        // the kernel's E tables hold l <= SQ_MAX_L_GRAD: refuse other bases
+        int *lh = (int *)malloc(sizeof(int) * basis->nshell);
+        if (!lh) return set_error(SQ_ERR_ARG, "sq_grad_1e: host allocation failed");
+        cudaError_t e = cudaMemcpyAsync(lh, basis->l, sizeof(int) * basis->nshell, cudaMemcpyDeviceToHost,
+                                        (cudaStream_t)stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+        int lmax = 0;
+        for (int s = 0; e == cudaSuccess && s < basis->nshell; ++s) lmax = lh[s] > lmax ? lh[s] : lmax;
+        free(lh);
+        if (e != cudaSuccess) return set_error(SQ_ERR_CUDA, "sq_grad_1e: %s", cudaGetErrorString(e));
+        if (lmax > SQ_MAX_L_GRAD)
+            return set_error(SQ_ERR_UNSUPPORTED, "sq_grad_1e: shell with l = %d > %d (no gradient kernel)", lmax,
+                             SQ_MAX_L_GRAD);
+    }
     grad1e_kernel<<<(np + 63) / 64, 64, 0, (cudaStream_t)stream>>>(*basis, table64, D, W, grad);
     return check_launch("sq_grad_1e");
 }

@@ -10,18 +10,19 @@ namespace sq {
 
 // ---------------------------------------------------------------------------
 // Boys grid: one thread per (grid point, order); compensated series sum.
-__global__ void boys_table_kernel(double *tab64, float *tab32) {
+// ngrid x ncol entries at out (last column exp(-T_k)); the FP32 copy is optional.
+__global__ void boys_table_kernel(double *out, float *out32, int ngrid, int ncol) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= SQ_BOYS_NGRID * SQ_BOYS_NCOL) return;
-    const int k = idx / SQ_BOYS_NCOL, m = idx % SQ_BOYS_NCOL;
+    if (idx >= ngrid * ncol) return;
+    const int k = idx / ncol, m = idx % ncol;
     const double T = k * (1.0 / SQ_BOYS_STEP_INV);
     double val;
-    if (m == SQ_BOYS_NCOL - 1) {
+    if (m == ncol - 1) {
         val = exp(-T);
     } else {
         // F_m(T) = e^{-T} sum_i (2T)^i / ((2m+1)(2m+3)...(2m+2i+1))
         double term = 1.0 / (2 * m + 1), sum = 0.0, comp = 0.0;
-        for (int i = 0; i < 400; ++i) {
+        for (int i = 0; i < 600; ++i) {
             const double y = term - comp;
             const double t = sum + y;
             comp = (t - sum) - y;
@@ -31,8 +32,8 @@ __global__ void boys_table_kernel(double *tab64, float *tab32) {
         }
         val = sum * exp(-T);
     }
-    tab64[idx] = val;
-    if (tab32) tab32[idx] = (float)val;
+    out[idx] = val;
+    if (out32) out32[idx] = (float)val;
 }
 
 // Scaled Taylor blocks from the finished F grid: F_{m+j}(T_k)/j! (m < 15) and
@@ -58,9 +59,11 @@ __global__ void boys_eval_kernel(int n_max, const double *z, long long nz, const
                                  double *out) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nz) return;
-    double F[SQ_BOYS_NCOL];
+    double F[SQ_BOYS_HI_NCOL];
     if (mode == 1) {
         for (int m = 0; m <= n_max; ++m) F[m] = boys_reference(m, z[i]);
+    } else if (mode == 2) {
+        for (int m = 0; m <= n_max; ++m) F[m] = boys_hi(m, z[i], tab);
     } else {
         boys64_rt(n_max, z[i], tab, F);
     }
@@ -395,7 +398,11 @@ using namespace sq;
 extern "C" int sq_boys_table(double *table64, float *table32, void *stream) {
     if (!table64) return set_error(SQ_ERR_ARG, "sq_boys_table: table64 is NULL");
     const int n = SQ_BOYS_NGRID * SQ_BOYS_NCOL;
-    boys_table_kernel<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(table64, table32);
+    boys_table_kernel<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(table64, table32, SQ_BOYS_NGRID,
+                                                                         SQ_BOYS_NCOL);
+    const int nh = SQ_BOYS_HI_NGRID * SQ_BOYS_HI_NCOL;
+    boys_table_kernel<<<(nh + 127) / 128, 128, 0, (cudaStream_t)stream>>>(table64 + SQ_BOYS_HI64_OFF, nullptr,
+                                                                          SQ_BOYS_HI_NGRID, SQ_BOYS_HI_NCOL);
     const int nt = 16 * SQ_BOYS_NGRID * 8;
     boys_taylor_kernel<<<(nt + 127) / 128, 128, 0, (cudaStream_t)stream>>>(table64, table32);
     return check_launch("sq_boys_table");
@@ -403,9 +410,10 @@ extern "C" int sq_boys_table(double *table64, float *table32, void *stream) {
 
 extern "C" int sq_boys(int n_max, const double *z, long long nz, const double *table64, int mode, double *out,
                        void *stream) {
-    if (!z || !table64 || !out || nz < 0 || (mode != 0 && mode != 1))
-        return set_error(SQ_ERR_ARG, "sq_boys: bad argument");
-    if (n_max < 0 || n_max > SQ_BOYS_NCOL - 1 - kBoysTaylor64) return set_error(SQ_ERR_ARG, "sq_boys: n_max out of range");
+    if (!z || !table64 || !out || nz < 0 || mode < 0 || mode > 2) return set_error(SQ_ERR_ARG, "sq_boys: bad argument");
+    const int limit = mode == 0 ? SQ_BOYS_NCOL - 1 - kBoysTaylor64
+                                : (mode == 2 ? SQ_BOYS_HI_NCOL - 1 - kBoysTaylor64 : SQ_BOYS_HI_NCOL - 2);
+    if (n_max < 0 || n_max > limit) return set_error(SQ_ERR_ARG, "sq_boys: n_max %d out of range 0..%d", n_max, limit);
     if (nz == 0) return SQ_OK;
     boys_eval_kernel<<<(unsigned)((nz + 127) / 128), 128, 0, (cudaStream_t)stream>>>(n_max, z, nz, table64, mode,
                                                                                   out);

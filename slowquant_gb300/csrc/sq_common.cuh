@@ -11,8 +11,8 @@
 
 #include "../../include/slowquant_gb300.h"
 
-#define SQ_LMAX 2            // highest shell angular momentum with compiled ERI kernels
-#define SQ_NPAIRCLASS 6      // (SQ_LMAX+1)(SQ_LMAX+2)/2 pair classes (la >= lb)
+#define SQ_LMAX 2            // highest shell angular momentum of the per-thread, warp and gradient
+                             // kernels; classes with f shells (up to SQ_MAX_L) run on eri_block.cu
 
 namespace sq {
 

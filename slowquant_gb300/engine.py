@@ -790,6 +790,9 @@ class IntegralEngine:
         the host.
         """
         self._require_eri()
+        if self.nshell and self.l.max() > _lib.SQ_MAX_L_GRAD:
+            raise NotImplementedError(
+                f"gradient kernels support shells up to l={_lib.SQ_MAX_L_GRAD}; basis has l={int(self.l.max())}")
         D = D.to(device=self.device, dtype=torch.float64).contiguous()
         S, T, V = self.one_electron()
         F = self.fock(T + V, D, threshold, "fp64")

@@ -45,7 +45,7 @@ def flops_per_contracted_quartet_jk(la: int, lb: int, lc: int, ld: int) -> int:
     return 12 * C(la) * C(lb) * C(lc) * C(ld)
 
 
-PAIR_CLASSES = [(0, 0), (1, 0), (1, 1), (2, 0), (2, 1), (2, 2)]
+PAIR_CLASSES = [(0, 0), (1, 0), (1, 1), (2, 0), (2, 1), (2, 2), (3, 0), (3, 1), (3, 2), (3, 3)]
 
 
 def quartet_class_l(qc: int):

@@ -27,7 +27,7 @@ from __future__ import annotations
 
 import numpy as np
 
-NQCLASS = 21
+NQCLASS = 55  # quartet classes of s, p, d and f shells (10 pair classes)
 
 
 def quartet_class(cb: int, ck: int) -> int:

@@ -173,6 +173,62 @@ def run_uhf_system(sq, name, geom, unit, basis, *, charge=0, mix=0.15, out=None)
     return res
 
 
+# H2O2 without symmetry (angstrom): two O centres carry f shells in cc-pVTZ.
+H2O2_ANGSTROM = """O   0.000000000000   0.000000000000   0.000000000000;
+           O   1.452000000000   0.081000000000   0.033000000000;
+           H  -0.262000000000   0.912000000000   0.187000000000;
+           H   1.698000000000  -0.457000000000   0.811000000000"""
+
+
+def f_shell_quartets(ref_eri, mol, budget_s: float = 1200.0) -> dict:
+    """Contracted blocks of shell quartets with f shells, from the reference's
+    electron_repulsion_integral (electronrepulsion.py:107-297).
+
+    Every class with an f shell that the basis offers is sampled: for each
+    (la, lb, lc, ld) with la >= lb, lc >= ld, (la,lb) >= (lc,ld) and max l = 3,
+    up to two quartets whose shells sit on different centres where possible,
+    cheapest first (the reference runs as plain Python here).
+    """
+    shells = mol.shells
+    ls = [int(s.angular_moments.sum(1)[0]) for s in shells]
+    atom = [mol.atoms.index(s.origin_atom) for s in shells]
+    npr = [len(s.exponents) for s in shells]
+    by_l = {l: [i for i in range(len(shells)) if ls[i] == l] for l in range(4)}
+    quartets = []
+    for la in range(4):
+        for lb in range(la + 1):
+            for lc in range(la + 1):
+                for ld in range(lc + 1):
+                    if (la, lb) < (lc, ld) or max(la, lb, lc, ld) < 3:
+                        continue
+                    cands = []
+                    for a in by_l[la]:
+                        for b in by_l[lb]:
+                            for c in by_l[lc]:
+                                for d in by_l[ld]:
+                                    ncent = len({atom[a], atom[b], atom[c], atom[d]})
+                                    cost = npr[a] * npr[b] * npr[c] * npr[d]
+                                    cands.append((-ncent, cost, (a, b, c, d)))
+                    cands.sort()
+                    quartets += [c[2] for c in cands[:2]]
+    keys, blocks = [], []
+    t0 = time.time()
+    for a, b, c, d in quartets:
+        if time.time() - t0 > budget_s:
+            break
+        s1, s2, s3, s4 = shells[a], shells[b], shells[c], shells[d]
+        V = ref_eri(s1.center, s2.center, s3.center, s4.center, s1.exponents, s2.exponents, s3.exponents,
+                    s4.exponents, s1.contraction_coefficients, s2.contraction_coefficients,
+                    s3.contraction_coefficients, s4.contraction_coefficients, s1.normalization,
+                    s2.normalization, s3.normalization, s4.normalization, s1.angular_moments,
+                    s2.angular_moments, s3.angular_moments, s4.angular_moments)
+        keys.append((a, b, c, d))
+        blocks.append(np.asarray(V).ravel())
+    off = np.concatenate([[0], np.cumsum([len(b) for b in blocks])]).astype(np.int64)
+    return {"quartets": np.array(keys, dtype=np.int64), "block_off": off, "blocks": np.concatenate(blocks),
+            "seconds": time.time() - t0}
+
+
 def boys_grid(ref_boys) -> dict:
     zs = np.concatenate([
         [0.0, 1e-12, 9.9e-11, 1.1e-10, 1e-8, 1e-6, 1e-4, 1e-3, 0.01],
@@ -228,6 +284,20 @@ def main() -> None:
         prim["ccpvdz_h2o_centers"] = mol.atom_coordinates
         np.savez_compressed(os.path.join(out, "primitives.npz"), **prim)
         print("primitives done", flush=True)
+
+    if want("h2o2_ccpvtz_f"):
+        from slowquant.molecularintegrals.electronrepulsion import electron_repulsion_integral
+
+        mol = _Molecule(H2O2_ANGSTROM, 0, "angstrom")
+        mol._set_basis_set("cc-pvtz")
+        res = f_shell_quartets(electron_repulsion_integral, mol)
+        secs = res.pop("seconds")
+        np.savez_compressed(os.path.join(out, "h2o2_ccpvtz_f.npz"), **res)
+        energies["h2o2_ccpvtz_f"] = {"basis": "cc-pvtz", "unit": "angstrom", "geometry": H2O2_ANGSTROM,
+                                     "nbf": int(mol.number_bf), "nshell": int(mol.number_shell),
+                                     "n_quartets": int(len(res["quartets"])), "seconds": round(secs, 2)}
+        json.dump(energies, open(energies_path, "w"), indent=1)
+        print("h2o2_ccpvtz_f", len(res["quartets"]), "quartets", round(secs, 1), "s", flush=True)
 
     systems = [
         ("h2o_sto3g_crawford", H2O_CRAWFORD_BOHR, "bohr", "sto-3g", dict(eri_store="full")),

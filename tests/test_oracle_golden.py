@@ -127,3 +127,35 @@ def test_oracle_uhf_matches_reference(name):
     if name in UHF_KNOWN:
         ref, tol = UHF_KNOWN[name]
         assert abs(E + m.nuclear_repulsion - ref) < tol
+
+
+@pytest.mark.parametrize("faithful", [True, False])
+def test_oracle_f_shell_quartets_match_reference(faithful, golden_energies):
+    """f shells (cc-pVTZ O): every f class of H2O2, two quartets each, against the reference's blocks."""
+    e = golden_energies["h2o2_ccpvtz_f"]
+    g = load_golden("h2o2_ccpvtz_f")
+    mol = O.OracleMolecule(e["geometry"], e["basis"], distance_unit=e["unit"])
+    assert mol.nbf == e["nbf"] == 100
+    classes = {tuple(sorted(len(mol.shells[s][3]) for s in q)) for q in g["quartets"]}
+    assert len(g["quartets"]) >= 60 and len(classes) > 10
+    out = mol.eri_quartets(g["quartets"], faithful=faithful)
+    assert np.max(np.abs(out - g["blocks"])) < 1e-14
+
+
+def test_reference_boys_truncation_on_f_shells(golden_energies):
+    """The reference's Boys series (integralfunctions.py:74-97) stops at the first
+    term below 1e-12 absolute; 1/(2n+1)!! < 1e-12 from n = 12 on, so the f-shell
+    blocks that the reference itself produced differ from the accurate function's
+    by up to ~1e-2.  The direct Fock build therefore uses the accurate Boys
+    function and is checked against the oracle's accurate mode."""
+    e = golden_energies["h2o2_ccpvtz_f"]
+    g = load_golden("h2o2_ccpvtz_f")
+    mol = O.OracleMolecule(e["geometry"], e["basis"], distance_unit=e["unit"])
+    O.lib().sqo_set_boys_mode(1)
+    try:
+        exact = mol.eri_quartets(g["quartets"])
+    finally:
+        O.lib().sqo_set_boys_mode(0)
+    dev = np.max(np.abs(exact - g["blocks"]))
+    assert 1e-4 < dev < 0.1, dev
+    assert O.boys(12, 5.0) == pytest.approx(np.exp(-5.0) / 25.0, rel=1e-14)
