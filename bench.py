@@ -138,7 +138,7 @@ def class_work(eng, ql, precision: str = "fp64") -> dict:
     """Per quartet class: contracted quartets, primitive quartets, model FLOPs.
 
     Primitive quartets are the ones the launch computes: the per-thread class
-    kernels (classes 0-18) loop over the slots' screened
+    kernels (classes 0-18, 21, 22, 28) loop over the slots' screened
     primitive pairs, the generic warp kernel over all of a pair's primitives.
     """
     import torch
@@ -158,7 +158,7 @@ def class_work(eng, ql, precision: str = "fp64") -> dict:
         a, b = int(ql.class_off[c]), int(ql.class_off[c + 1])
         if b == a:
             continue
-        per_thread = c <= 18
+        per_thread = c <= 18 or c in (21, 22, 28)  # the per-thread kernels (f: (fs|ss), (fs|ps), (fp|ss))
         npp = npp_slot if per_thread else npp_all
         seg = ql.pairs[a:b].long()
         nprim = int((npp[seg[:, 0]] * npp[seg[:, 1]]).sum())
@@ -430,7 +430,7 @@ def gpu_arm(args) -> None:
     rows = []
     for lst, prec, work in ((q64, "fp64", work64), (q32, "fp32", work32)):
         for c, w in work.items():
-            off = np.zeros(22, dtype=np.int64)
+            off = np.zeros(_lib.SQ_MAX_QCLASS + 1, dtype=np.int64)
             off[c + 1:] = w["list_entries"]
             sub = QuartetList(lst.pairs[lst.class_off[c]:lst.class_off[c + 1]], off)
             eng.jk_accumulate(D, [sub], [prec])

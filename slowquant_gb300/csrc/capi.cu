@@ -28,6 +28,7 @@ int check_launch(const char *what) {
 
 #define DECL(QC) cudaError_t launch_qc_##QC(const EriArgs &, int, int, cudaStream_t);
 DECL(0) DECL(1) DECL(2) DECL(3) DECL(4) DECL(5) DECL(6) DECL(7) DECL(8) DECL(9) DECL(10) DECL(11)
+DECL(21) DECL(22) DECL(28)
 #undef DECL
 #define DECL32(QC) cudaError_t launch_qc_##QC##_f32(const EriArgs &, int, int, cudaStream_t);
 DECL32(12) DECL32(13) DECL32(14) DECL32(15) DECL32(16) DECL32(17) DECL32(18)
@@ -58,15 +59,18 @@ static const eri_launcher kLaunchersF64[SQ_MAX_QCLASS] = {
 };
 
 // Per-thread (fully unrolled) J/K kernels exist for the light classes (L <= 4,
-// except (dd|ss)) in every precision, and for classes 12-18 in SQ_FP64 and
-// SQ_FP32; every other class/precision of s, p and d shells, and every
-// dense-tensor or Schwarz launch of those, runs on the generic warp kernel.
-// Classes 21-54 (with an f shell) always run on the block kernel.
+// except (dd|ss); with f: (fs|ss), (fs|ps), (fp|ss)) in every precision, and
+// for classes 12-18 in SQ_FP64 and SQ_FP32.  Every other launch runs on the
+// generic warp kernel when its blocks fit the warp kernel's tables (s, p, d
+// shells, and bra pairs (fs), (fp): at most 36 components per pair, L <= 8),
+// else on the block kernel ((fd|..), (ff|..)).
 // SQ_OPT_GENERIC_MIN_L = 0 sends everything to it.
 static const eri_launcher kLaunchers[SQ_MAX_QCLASS] = {
-    launch_qc_0, launch_qc_1, launch_qc_2, launch_qc_3, launch_qc_4, launch_qc_5, launch_qc_6,
-    launch_qc_7, launch_qc_8, launch_qc_9, launch_qc_10, launch_qc_11, nullptr, nullptr,
-    nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+    launch_qc_0,  launch_qc_1,  launch_qc_2, launch_qc_3, launch_qc_4, launch_qc_5, launch_qc_6,
+    launch_qc_7,  launch_qc_8,  launch_qc_9, launch_qc_10, launch_qc_11, nullptr, nullptr,
+    nullptr,      nullptr,      nullptr,     nullptr,     nullptr,     nullptr,     nullptr,
+    launch_qc_21, launch_qc_22, nullptr,     nullptr,     nullptr,     nullptr,     nullptr,
+    launch_qc_28,
 };
 
 // Angular momenta of pair class pc (la >= lb).
@@ -169,9 +173,9 @@ static cudaError_t launch_class(EriArgs &args, const sq_quartets *qs, int c, int
         args.cfg_threads = 0;
         args.cfg_blocks = 0;
     }
-    if (la > SQ_LMAX || lb > SQ_LMAX || lc > SQ_LMAX || ld > SQ_LMAX)
-        return launch_eri_block(args, la, lb, lc, ld, mode, precision, stream);
     const int L = la + lb + lc + ld;
+    const bool warp_fits = ncart(la) * ncart(lb) <= ncart(SQ_LMAX) * ncart(SQ_LMAX) &&
+                           ncart(lc) * ncart(ld) <= ncart(SQ_LMAX) * ncart(SQ_LMAX) && L <= 4 * SQ_LMAX;
     eri_launcher unrolled = nullptr;
     if (mode == MODE_JK && L < g_generic_min_l) unrolled = kLaunchers[c];
     if (mode == MODE_JK && precision == SQ_FP32 && kLaunchersF32[c] != nullptr && g_generic_min_l > 0)
@@ -180,6 +184,7 @@ static cudaError_t launch_class(EriArgs &args, const sq_quartets *qs, int c, int
         ((g_fp64_unrolled_high >> c) & 1))
         unrolled = kLaunchersF64[c];
     if (unrolled != nullptr) return unrolled(args, mode, precision, stream);
+    if (!warp_fits) return launch_eri_block(args, la, lb, lc, ld, mode, precision, stream);
     return launch_eri_warp(args, WarpClass{la, lb, lc, ld}, mode, precision, stream);
 }
 

@@ -45,10 +45,16 @@ struct WarpSmem {
 };
 
 // J/K epilogue scratch (FP64), overlaid on a warp's shared memory after its
-// primitive loops: the integral block, then the six density blocks.  A warp's
-// slice is the larger of the two uses, rounded to 16 bytes.
+// primitive loops: the integral block, then the six density blocks, each at
+// the class's own size.  A warp's slice is the larger of the two uses, rounded
+// to 16 bytes; kWarpEpi is the (dd|dd) need, which also covers the f classes
+// that run here ((fp|dd): 1302 doubles).
 constexpr int kWarpBlk = ncart(SQ_LMAX) * ncart(SQ_LMAX);
 constexpr int kWarpEpi = kWarpBlk * kWarpBlk + 6 * kWarpBlk;
+__host__ __device__ constexpr int warp_epi_size(int la, int lb, int lc, int ld) {
+    return ncart(la) * ncart(lb) * ncart(lc) * ncart(ld) + ncart(la) * ncart(lb) + ncart(lc) * ncart(ld) +
+           ncart(la) * ncart(lc) + ncart(lb) * ncart(ld) + ncart(la) * ncart(ld) + ncart(lb) * ncart(lc);
+}
 template <typename R>
 __host__ __device__ constexpr size_t warp_stride() {
     return ((sizeof(WarpSmem<R>) > kWarpEpi * sizeof(double) ? sizeof(WarpSmem<R>) : kWarpEpi * sizeof(double)) +
@@ -335,14 +341,15 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
             if (P == Q) m *= 0.5;
             const double wJ = 0.5 * m, wK = 0.25 * m;
             const sq_basis &bs = args.basis;
+            // packed at the class's own sizes (warp_epi_size <= kWarpEpi, checked at launch)
             double *ep = reinterpret_cast<double *>(&sm);
-            double *Vb = ep;                          // [NAB][NCD]
-            double *Dab = ep + kWarpBlk * kWarpBlk;   // [NA][NB]
-            double *Dcd = Dab + kWarpBlk;             // [NC][ND]
-            double *Dac = Dcd + kWarpBlk;             // [NA][NC]
-            double *Dbd = Dac + kWarpBlk;             // [NB][ND]
-            double *Dad = Dbd + kWarpBlk;             // [NA][ND]
-            double *Dbc = Dad + kWarpBlk;             // [NB][NC]
+            double *Vb = ep;                 // [NAB][NCD]
+            double *Dab = ep + NACC;         // [NA][NB]
+            double *Dcd = Dab + NAB;         // [NC][ND]
+            double *Dac = Dcd + NCD;         // [NA][NC]
+            double *Dbd = Dac + NA * NC;     // [NB][ND]
+            double *Dad = Dbd + NB * ND;     // [NA][ND]
+            double *Dbc = Dad + NA * ND;     // [NB][NC]
             __syncwarp();
 #pragma unroll
             for (int kk = 0; kk < KACC; ++kk)
@@ -445,6 +452,12 @@ constexpr size_t warp_smem_bytes() {
 inline cudaError_t launch_eri_warp(const EriArgs &args, const WarpClass &cls, int mode, int precision,
                                    cudaStream_t stream) {
     if (args.nq <= 0) return cudaSuccess;
+    // the class must fit the per-warp tables (Hermite entries, W, accumulators, epilogue)
+    const int nab = ncart(cls.la) * ncart(cls.lb), ncd = ncart(cls.lc) * ncart(cls.ld);
+    const int L = cls.la + cls.lb + cls.lc + cls.ld;
+    if (nab > kWarpBlk || ncd > kWarpBlk || L > 4 * SQ_LMAX || nherm(cls.la + cls.lb) * ncd > kWarpWmax ||
+        warp_epi_size(cls.la, cls.lb, cls.lc, cls.ld) > kWarpEpi)
+        return cudaErrorInvalidValue;
     long long blocks = (args.nq + kWarpsPerBlock - 1) / kWarpsPerBlock;
     const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : 152LL * 64;
     if (blocks > cap) blocks = cap;

@@ -260,3 +260,25 @@ def test_gradient_refuses_f_shells(h2o2):
                         _lib.stream_handle())
     assert rc == _lib.SQ_ERR_UNSUPPORTED
     assert float(grad.abs().sum()) == 0.0
+
+
+def test_f_classes_agree_across_kernel_shapes(h2o2):
+    """(fs|ss), (fs|ps), (fp|ss) on per-thread kernels == on the warp kernel (all precisions)."""
+    import torch
+
+    from slowquant_gb300 import _lib
+
+    e, eng = h2o2
+    D = torch.tensor(_random_density(eng.nbf, 4), dtype=torch.float64, device="cuda")
+    lib = _lib.lib()
+    res = {}
+    try:
+        for min_l in (5, 0):
+            lib.sq_set_option(_lib.SQ_OPT_GENERIC_MIN_L, min_l)
+            res[min_l] = {p: [x.cpu().numpy() for x in eng.jk(D, 1e-12, p, fp32_threshold=1e30)]
+                          for p in ("fp64", "mixed", "mixed_boys32")}
+    finally:
+        lib.sq_set_option(_lib.SQ_OPT_GENERIC_MIN_L, 5)
+    for p, tol in (("fp64", 1e-11), ("mixed", 2e-4), ("mixed_boys32", 2e-4)):
+        for a, b in zip(res[5][p], res[0][p]):
+            assert np.max(np.abs(a - b)) < tol, p
