@@ -25,7 +25,7 @@ import torch
 
 from . import _lib, screening
 from ._lib import SqBasis, SqPairs, SqQuartets, SqSlots, check, ptr
-from .engine import CLASS_WEIGHT, SPLIT_TARGET, QuartetList, herm_size
+from .engine import CLASS_WEIGHT, F_PER_THREAD, SPLIT_TARGET, QuartetList, herm_size
 from .molecule import _Molecule
 
 
@@ -271,7 +271,7 @@ class BatchEngine:
         # FP64 classes 12-18 split only while all of them run on per-thread kernels
         mask = int(self.lib.sq_get_option(_lib.SQ_OPT_FP64_UNROLLED_HIGH))
         hi = 18 if all((mask >> c) & 1 for c in range(12, 19)) else 11
-        split_max = [hi, hi]
+        split_set = frozenset(range(hi + 1)) | F_PER_THREAD
         merged = [{c: [] for c in range(screening.NQCLASS)} for _ in range(nl)]
         for mi in range(self.nmol):
             sel = np.nonzero(self.pair_mol == mi)[0]
@@ -287,7 +287,7 @@ class BatchEngine:
                         bslots = self.slot_of_pair[sel[bra]]
                         # heavy quartets of the per-thread classes: bra sub-slot chunks
                         S = 1
-                        if c <= split_max[li]:
+                        if c in split_set:
                             while cost * CLASS_WEIGHT[c] > SPLIT_TARGET * S and (2 * S) in self.sub_first and \
                                     self.sub_first[2 * S][bslots[0]] >= 0:
                                 S *= 2

@@ -50,6 +50,8 @@ PRIM_SCREEN = 1e-17
 SPLIT_TARGET = 512
 # primitive pairs per chunk (at least) in the per-chunk precision mode
 CHUNK_MIN = 2
+# f-shell classes with per-thread J/K kernels in every precision: (fs|ss), (fs|ps), (fp|ss)
+F_PER_THREAD = frozenset({21, 22, 28})
 _W_SSSS = flops.flops_per_primitive_quartet(0, 0, 0, 0)
 CLASS_WEIGHT = [flops.flops_per_primitive_quartet(*flops.quartet_class_l(c)) / _W_SSSS
                 for c in range(screening.NQCLASS)]
@@ -474,9 +476,9 @@ class IntegralEngine:
         is applied per bra chunk of the FP64 quartets of the per-thread classes:
         a chunk goes to FP32 when the sum of its primitive Schwarz factors times
         the ket's is below fp32_threshold."""
-        hi = self._fp64_per_thread_max()
+        s64, s32 = self._split_classes()
         key = (float(threshold), None if fp32_threshold is None else float(fp32_threshold), bool(split),
-               bool(chunks), hi)
+               bool(chunks), s64)
         if q is None and key in self._quartet_cache:
             return self._quartet_cache[key]
         self._require_eri()
@@ -486,16 +488,23 @@ class IntegralEngine:
         lists, ket_list = screening.build_tasks(self.pair_class, npp_eff, np.ones_like(npp_eff), qv, threshold,
                                                 fp32_threshold)
         self.slots  # canonical slot numbering (from the engine's own Schwarz factors)
-        # classes with per-thread kernels: 0-18 (FP64: 12-18 unless switched off) and FP32 0-18
-        split_max = [hi, 18] if split else [-1, -1]
+        # classes with per-thread kernels: 0-18 (FP64: 12-18 unless switched off), FP32 0-18,
+        # and the light f classes in both
+        split_sets = [s64, s32] if split else [frozenset(), frozenset()]
         if chunks and fp32_threshold is not None:
-            out = self._chunk_lists(lists, ket_list, float(fp32_threshold), hi)
+            out = self._chunk_lists(lists, ket_list, float(fp32_threshold), s64)
         else:
-            out = [self._expand(t, ket_list, split_max[li]) for li, t in enumerate(lists)]
+            out = [self._expand(t, ket_list, split_sets[li]) for li, t in enumerate(lists)]
         res = out[0] if len(out) == 1 else (out[0], out[1])
         if own:
             self._quartet_cache[key] = res
         return res
+
+    def _split_classes(self):
+        """(FP64, FP32) sets of the classes whose J/K quartets may be split into
+        sub-slot chunks: those on per-thread kernels in that precision."""
+        hi = self._fp64_per_thread_max()
+        return frozenset(range(hi + 1)) | F_PER_THREAD, frozenset(range(19)) | F_PER_THREAD
 
     def _fp64_per_thread_max(self) -> int:
         """Highest class index up to which every FP64 J/K launch runs on a per-thread kernel
@@ -505,17 +514,19 @@ class IntegralEngine:
         mask = int(self.lib.sq_get_option(_lib.SQ_OPT_FP64_UNROLLED_HIGH))
         return 18 if all((mask >> c) & 1 for c in range(12, 19)) else 11
 
-    def _chunk_lists(self, lists, ket_list: np.ndarray, tau: float, hi: int = 18):
+    def _chunk_lists(self, lists, ket_list: np.ndarray, tau: float, split64=None):
         """(FP64, FP32) lists with the precision test per bra primitive chunk.
 
-        FP64 quartets of the per-thread classes (0-18) are cut into S chunks of
+        FP64 quartets of the per-thread classes (split64: 0-18 and F_PER_THREAD) are cut into S chunks of
         their bra's primitive pairs (sorted by descending factor, CHUNK_MIN to
         2 CHUNK_MIN per chunk, more when the quartet is heavy), kets are cut the same way where
         a ket straddles the threshold, and each (bra chunk, ket chunk) is placed
         by its own bound; FP32 quartets stay whole.
         """
         t64, t32 = lists
-        q32 = self._expand(t32, ket_list, hi)
+        if split64 is None:
+            split64 = self._split_classes()[0]
+        q32 = self._expand(t32, ket_list, split64)
         npp = self.slot_npp
         ket_slots = self.slot_of_pair[ket_list]
         keep64 = {c: [] for c in range(screening.NQCLASS)}
@@ -524,7 +535,7 @@ class IntegralEngine:
         for c in range(screening.NQCLASS):
             for m, st, n in t64[c]:
                 slots = self.slot_of_pair[m]
-                if c > hi or len(m) == 0:
+                if c not in split64 or len(m) == 0:
                     whole64[c].append((m, st, n))  # pair ids: _expand maps them to slots
                     continue
                 nb = int(npp[slots[0]])
@@ -546,7 +557,7 @@ class IntegralEngine:
                 move32[c].append(k32)
         # FP64 list: whole-quartet blocks of the warp classes (device expand) and
         # the kept chunks; FP32 list: the quartet-level FP32 list plus the moved chunks
-        q64w = self._expand(whole64, ket_list, -1)
+        q64w = self._expand(whole64, ket_list)
         dev = self.device
 
         def merge(base, extra):
@@ -608,7 +619,7 @@ class IntegralEngine:
         cat = lambda xs: np.concatenate(xs).astype(np.int32) if xs else np.zeros((0, 2), np.int32)  # noqa: E731
         return cat(out64), cat(out32)
 
-    def _split_tasks(self, tasks: dict, ket_list: np.ndarray, split_max_class: int) -> dict:
+    def _split_tasks(self, tasks: dict, ket_list: np.ndarray, split_classes=frozenset()) -> dict:
         """Bra slot ids of every task block, heavy blocks replaced by their sub-slot chunks."""
         npp = self.slot_npp
         out = {}
@@ -616,7 +627,7 @@ class IntegralEngine:
             blocks = []
             for m, st, n in tasks[c]:
                 slots = self.slot_of_pair[m]
-                if c <= split_max_class and len(m):
+                if c in split_classes and len(m):
                     cost = int(npp[slots[0]]) * int(npp[self.slot_of_pair[ket_list[st[0]]]]) * CLASS_WEIGHT[c]
                     S = 1
                     while cost > SPLIT_TARGET * S and (2 * S) in self.sub_first and \
@@ -631,8 +642,8 @@ class IntegralEngine:
             out[c] = blocks
         return out
 
-    def _expand(self, tasks: dict, ket_list: np.ndarray, split_max_class: int = -1) -> QuartetList:
-        bra, kst, cnt, toff, off = screening.flatten_tasks(self._split_tasks(tasks, ket_list, split_max_class))
+    def _expand(self, tasks: dict, ket_list: np.ndarray, split_classes=frozenset()) -> QuartetList:
+        bra, kst, cnt, toff, off = screening.flatten_tasks(self._split_tasks(tasks, ket_list, split_classes))
         nq = int(off[-1])
         dev = self.device
         pairs = torch.empty((max(nq, 1), 2), dtype=torch.int32, device=dev)
