@@ -31,6 +31,8 @@ sys.path.insert(0, ROOT)
 METRIC = "ERI quartets/s & Fock-build ms, mixed vs FP64 plain on GPU at |ΔE|≤1e-6 Eh"
 WATERS, BOX, SEED, BASIS = 16, 11.0, 16, "cc-pvdz"
 BOXES = {16: 11.0, 8: 9.0}
+# Cartesian basis functions per water and the basis's name as printed
+BASES = {"cc-pvdz": (25, "cc-pVDZ"), "cc-pvtz": (65, "cc-pVTZ")}
 SCREEN, FP32_THR = 1e-12, 1e-4
 
 
@@ -41,11 +43,12 @@ def workload_geometry() -> str:
 
 
 def config(extra=None) -> dict:
+    nbf_w, label = BASES[BASIS]
     c = {
-        "workload": f"(H2O)_{WATERS} cc-pVDZ Fock build (J+K), {25 * WATERS} Cartesian bf, "
+        "workload": f"(H2O)_{WATERS} {label} Fock build (J+K), {nbf_w * WATERS} Cartesian bf, "
                     f"{BOXES.get(WATERS, BOX):g} A cube seed {SEED}",
         "molecule": f"(H2O)_{WATERS}",
-        "basis": f"cc-pVDZ (Cartesian, {25 * WATERS} bf)",
+        "basis": f"{label} (Cartesian, {nbf_w * WATERS} bf)",
         "schwarz_threshold": SCREEN,
         "fp32_schwarz_threshold": FP32_THR,
         "precision": "mixed (FP32 quartets below bound 1e-4, FP64 Boys recursion; FP64 above)",
@@ -632,6 +635,8 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--waters", type=int, default=16, choices=[8, 16],
                     help="cluster size (16 is the benchmark workload; 8 for quick profiling)")
+    ap.add_argument("--basis", default="cc-pvdz", choices=sorted(BASES),
+                    help="cc-pvdz is the benchmark workload; cc-pvtz adds f shells on O (secondary line)")
     ap.add_argument("--workload", default="fock", choices=["fock", "batch", "gradient"],
                     help="fock: the headline Fock-build line; batch / gradient: secondary measurements")
     ap.add_argument("--batch-size", type=int, default=256)
@@ -639,8 +644,9 @@ def main() -> None:
     ap.add_argument("--tau-sweep", type=float, nargs="*", default=[1e-5, 1e-4, 1e-3, 1e-2, 1e-1],
                     help="FP32 Schwarz thresholds reported beside the headline (empty: skip)")
     args = ap.parse_args()
-    global WATERS, SEED
+    global WATERS, SEED, BASIS
     WATERS = SEED = args.waters
+    BASIS = args.basis
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
