@@ -217,3 +217,84 @@ def test_ket_chunk_partition():
     for b, k in entries:
         want[(b, k)] = want.get((b, k), 0) + int(npp[k])
     assert got == want
+
+
+def _header_defines():
+    """Integer #defines of the public header, expressions evaluated in order."""
+    text = open(os.path.join(ROOT, "include", "slowquant_gb300.h")).read()
+    vals = {}
+    for name, expr in re.findall(r"^#define\s+(SQ_\w+)\s+([^/\n]+)", text, flags=re.M):
+        expr = expr.strip()
+        try:
+            vals[name] = eval(expr, {"__builtins__": {}}, dict(vals))
+        except (NameError, SyntaxError):
+            continue
+    return vals
+
+
+def test_header_constants_match_python_bindings():
+    from slowquant_gb300 import _lib
+
+    d = _header_defines()
+    names = [n for n in dir(_lib) if n.startswith("SQ_") and isinstance(getattr(_lib, n), (int, float))]
+    assert len(names) > 20
+    for n in names:
+        if n in d:
+            assert getattr(_lib, n) == d[n], n
+    for n in ("SQ_MAX_L", "SQ_MAX_QCLASS", "SQ_MAX_L_GRAD", "SQ_BOYS_TAB64_SIZE", "SQ_BOYS_TAB32_SIZE",
+              "SQ_BOYS_HI64_OFF", "SQ_ERR_UNSUPPORTED", "SQ_OPT_JK_STREAMS"):
+        assert n in d and getattr(_lib, n) == d[n], n
+    # 10 pair classes (la >= lb, l <= 3) -> 55 quartet classes; the grids fit the orders used
+    npc = (d["SQ_MAX_L"] + 1) * (d["SQ_MAX_L"] + 2) // 2
+    assert d["SQ_MAX_QCLASS"] == npc * (npc + 1) // 2
+    assert d["SQ_BOYS_HI_NCOL"] - 1 >= 4 * d["SQ_MAX_L"] + 7  # F_m + 6 Taylor orders + exp column
+    assert (d["SQ_BOYS_HI_NGRID"] - 1) / d["SQ_BOYS_STEP_INV"] >= d["SQ_BOYS_HI_TMAX"] + 0.5 / d["SQ_BOYS_STEP_INV"]
+
+
+def test_ctypes_structs_match_c_layout(tmp_path):
+    """sizeof / offsetof of every ABI struct, from gcc on the public header, equal the ctypes mirrors."""
+    import shutil
+    import subprocess
+
+    from slowquant_gb300 import _lib
+
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    structs = {"sq_basis": _lib.SqBasis, "sq_pairs": _lib.SqPairs, "sq_slots": _lib.SqSlots,
+               "sq_quartets": _lib.SqQuartets}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "slowquant_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "abi.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "abi"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    out = subprocess.check_output([str(exe)], text=True).split("\n")
+    for line in out:
+        if not line:
+            continue
+        cname, field, val = line.split()
+        py = structs[cname]
+        want = ctypes.sizeof(py) if field == "size" else getattr(py, field).offset
+        assert int(val) == want, (cname, field)
+
+
+def test_quartet_class_indexing_covers_f():
+    from slowquant_gb300 import engine, flops, screening
+
+    assert screening.NQCLASS == 55 and len(engine.CLASS_WEIGHT) == 55
+    seen = set()
+    for c in range(screening.NQCLASS):
+        la, lb, lc, ld = flops.quartet_class_l(c)
+        assert la >= lb and lc >= ld and engine.pair_class(la, lb) >= engine.pair_class(lc, ld)
+        assert screening.quartet_class(engine.pair_class(la, lb), engine.pair_class(lc, ld)) == c
+        seen.add((la, lb, lc, ld))
+    assert len(seen) == 55
+    assert sum(1 for c in range(55) if max(flops.quartet_class_l(c)) == 3) == 34
+    assert all(max(flops.quartet_class_l(c)) <= 2 for c in range(21))
+    assert engine.F_PER_THREAD == {21, 22, 28}
+    assert [flops.quartet_class_l(c) for c in sorted(engine.F_PER_THREAD)] == [(3, 0, 0, 0), (3, 0, 1, 0),
+                                                                              (3, 1, 0, 0)]
