@@ -292,9 +292,17 @@ def main() -> None:
         mol._set_basis_set("cc-pvtz")
         res = f_shell_quartets(electron_repulsion_integral, mol)
         secs = res.pop("seconds")
+        from slowquant.molecularintegrals.kineticenergy import kinetic_energy_integral_driver
+        from slowquant.molecularintegrals.multipole import multipole_integral_driver
+        from slowquant.molecularintegrals.nuclearattraction import nuclear_attraction_integral_driver
+
+        res["S"] = multipole_integral_driver(mol, np.array([0, 0, 0]))
+        res["T"] = kinetic_energy_integral_driver(mol)
+        res["V"] = nuclear_attraction_integral_driver(mol)
         np.savez_compressed(os.path.join(out, "h2o2_ccpvtz_f.npz"), **res)
         energies["h2o2_ccpvtz_f"] = {"basis": "cc-pvtz", "unit": "angstrom", "geometry": H2O2_ANGSTROM,
                                      "nbf": int(mol.number_bf), "nshell": int(mol.number_shell),
+                                     "E_nuc": float(mol.nuclear_repulsion),
                                      "n_quartets": int(len(res["quartets"])), "seconds": round(secs, 2)}
         json.dump(energies, open(energies_path, "w"), indent=1)
         print("h2o2_ccpvtz_f", len(res["quartets"]), "quartets", round(secs, 1), "s", flush=True)

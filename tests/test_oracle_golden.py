@@ -140,6 +140,12 @@ def test_oracle_f_shell_quartets_match_reference(faithful, golden_energies):
     assert len(g["quartets"]) >= 60 and len(classes) > 10
     out = mol.eri_quartets(g["quartets"], faithful=faithful)
     assert np.max(np.abs(out - g["blocks"])) < 1e-14
+    # one-electron matrices and nuclear repulsion of the same f basis
+    S, T, V = mol.one_electron()
+    np.testing.assert_allclose(S, g["S"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(T, g["T"], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(V, g["V"], rtol=0, atol=1e-12)
+    assert abs(mol.nuclear_repulsion - e["E_nuc"]) < 1e-12
 
 
 def test_reference_boys_truncation_on_f_shells(golden_energies):
