@@ -79,11 +79,12 @@ def _brute_force(pc, q, thr):
     return out
 
 
-@pytest.mark.parametrize("seed", [0, 1, 2])
-def test_quartet_lists_unique_and_complete(seed):
+@pytest.mark.parametrize("seed,npc", [(0, 6), (1, 6), (2, 6), (3, 10), (4, 10)])
+def test_quartet_lists_unique_and_complete(seed, npc):
+    """npc = 6: s, p, d pair classes; 10: with the f pair classes (quartet classes up to 54)."""
     rng = np.random.default_rng(seed)
     n = 60
-    pc = np.sort(rng.integers(0, 6, n)).astype(np.int32)
+    pc = np.sort(rng.integers(0, npc, n)).astype(np.int32)
     npa = rng.choice([1, 3, 8], n)
     npb = rng.choice([1, 3], n)
     q = 10.0 ** rng.uniform(-9, 0.5, n)
