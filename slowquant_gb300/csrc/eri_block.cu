@@ -24,7 +24,6 @@
 #include "boys.cuh"
 #include "capi_internal.cuh"
 #include "eri.cuh"
-#include "eri_warp.cuh"
 
 namespace sq {
 

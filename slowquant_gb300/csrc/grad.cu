@@ -22,7 +22,6 @@
 #include "boys.cuh"
 #include "capi_internal.cuh"
 #include "eri.cuh"
-#include "eri_warp.cuh"
 
 namespace sq {
 

@@ -112,4 +112,43 @@ __device__ __forceinline__ float d2f_bits(double x) {
     return __uint_as_float(sign | (e2 << 23) | m23);
 }
 
+// Index helpers of the runtime-class kernels (warp, block and gradient kernels).
+//
+// Flat Hermite index: degree n = t+u+v ascending, then t descending, then u descending.
+__host__ __device__ __forceinline__ int herm_index(int t, int u, int v) {
+    const int n = t + u + v;
+    return n * (n + 1) * (n + 2) / 6 + (n - t) * (n - t + 1) / 2 + (n - t - u);
+}
+
+__device__ __forceinline__ void cart_powers(int l, int c, int &x, int &y, int &z) {
+    int idx = 0;
+    for (int xx = l; xx >= 0; --xx)
+        for (int yy = l - xx; yy >= 0; --yy) {
+            if (idx == c) {
+                x = xx;
+                y = yy;
+                z = l - xx - yy;
+                return;
+            }
+            ++idx;
+        }
+    x = y = z = 0;
+}
+
+__device__ __forceinline__ int herm_offset_rt(int la, int lb, int a, int b) {
+    const int nb = ncart(lb);
+    int off = 0;
+    for (int aa = 0; aa < ncart(la); ++aa) {
+        int ax, ay, az;
+        cart_powers(la, aa, ax, ay, az);
+        for (int bb = 0; bb < nb; ++bb) {
+            if (aa == a && bb == b) return off;
+            int bx, by, bz;
+            cart_powers(lb, bb, bx, by, bz);
+            off += (ax + bx + 1) * (ay + by + 1) * (az + bz + 1);
+        }
+    }
+    return off;
+}
+
 }  // namespace sq
