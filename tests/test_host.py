@@ -299,3 +299,42 @@ def test_quartet_class_indexing_covers_f():
     assert engine.F_PER_THREAD == {21, 22, 28}
     assert [flops.quartet_class_l(c) for c in sorted(engine.F_PER_THREAD)] == [(3, 0, 0, 0), (3, 0, 1, 0),
                                                                               (3, 1, 0, 0)]
+
+
+def test_abi_refuses_bad_arguments_before_touching_the_device():
+    """Argument errors come back as status codes with a message (no device work is started)."""
+    from slowquant_gb300 import _lib, build
+
+    if not os.path.exists(_lib.LIB_PATH):
+        build.build()
+    L = _lib.lib()
+    defaults = {k: L.sq_get_option(k) for k in (_lib.SQ_OPT_GENERIC_MIN_L, _lib.SQ_OPT_JK_STREAMS,
+                                                _lib.SQ_OPT_FP64_UNROLLED_HIGH, _lib.SQ_OPT_GRAD_THREAD)}
+    try:
+        assert defaults[_lib.SQ_OPT_JK_STREAMS] == 8 and defaults[_lib.SQ_OPT_GENERIC_MIN_L] == 5
+        assert defaults[_lib.SQ_OPT_FP64_UNROLLED_HIGH] == 0x7F << 12
+        assert L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, 0) == _lib.SQ_ERR_ARG
+        assert L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, 17) == _lib.SQ_ERR_ARG
+        assert L.sq_set_option(_lib.SQ_OPT_FP64_UNROLLED_HIGH, 1 << _lib.SQ_MAX_QCLASS) == _lib.SQ_ERR_ARG
+        assert L.sq_set_option(99, 1) == _lib.SQ_ERR_ARG
+        assert b"unknown key" in L.sq_last_error()
+        assert L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, 3) == _lib.SQ_OK and L.sq_get_option(_lib.SQ_OPT_JK_STREAMS) == 3
+        assert L.sq_set_launch_config(_lib.SQ_MAX_QCLASS, 0, 64, 100) == _lib.SQ_ERR_ARG
+        assert L.sq_set_launch_config(_lib.SQ_MAX_QCLASS - 1, 0, 48, 100) == _lib.SQ_ERR_ARG
+        assert L.sq_set_launch_config(_lib.SQ_MAX_QCLASS - 1, 0, 0, 0) == _lib.SQ_OK  # back to the built-in shape
+        buf = (ctypes.c_double * 64)()
+        p = ctypes.addressof(buf)
+        assert L.sq_boys(2, None, 1, p, 0, p, None) == _lib.SQ_ERR_ARG
+        assert L.sq_boys(9, p, 1, p, 0, p, None) == _lib.SQ_ERR_ARG  # beyond the d grid
+        assert L.sq_boys(17, p, 1, p, 2, p, None) == _lib.SQ_ERR_ARG  # beyond the high-order grid
+        assert L.sq_boys(2, p, 1, p, 3, p, None) == _lib.SQ_ERR_ARG  # unknown mode
+        L.sq_boys(9, p, 1, p, 0, p, None)
+        assert b"n_max 9 out of range" in L.sq_last_error()
+        assert L.sq_jk(None, None, None, None, None, None, None, None, None, None, 0, None) == _lib.SQ_ERR_ARG
+        assert b"NULL" in L.sq_last_error()
+        assert L.sq_grad_2e(None, None, None, None, None, None, None, None) == _lib.SQ_ERR_ARG
+        assert L.sq_batched_eigh(1, p, p, 129, p, p, p, p, 1e-12, 10, None, None) == _lib.SQ_ERR_ARG
+        assert b"dimension" in L.sq_last_error()
+    finally:
+        for k, v in defaults.items():
+            L.sq_set_option(k, v)
