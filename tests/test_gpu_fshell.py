@@ -67,8 +67,7 @@ def test_boys_high_order_grid(gpu_lib):
             O.lib().sqo_set_boys_mode(0)
 
     # exact F_n: the series below z = 1, else Gamma(n+1/2) P(n+1/2, z) / (2 z^{n+1/2})
-    # (the oracle's own accurate mode switches to the asymptote at z = 40, which
-    # is 4e-7 off at n = 12 there)
+    # (an asymptote from z = 40 on would be 4e-7 off at n = 12 there)
     from scipy.special import gamma, gammainc
 
     exact = oracle(16, 1)
