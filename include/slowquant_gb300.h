@@ -258,16 +258,20 @@ int sq_jk_multi(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *sl
 /* J/K build for callers that cannot allocate device memory.  No counterpart
  * in the reference (it has no device code).  Same arguments and results as
  * sq_jk, minus D32: the FP32 density scratch that FP32 launches need lives in
- * a fixed array inside this library (SQ_NOALLOC_MAX_NBF^2 floats, 4 MiB, held
+ * a fixed array inside this library (SQ_NOALLOC_MAX_ELEMS floats, 4 MiB, held
  * on every GPU that loads the library until the process exits).  It serves
  * hosts that own all device memory, streams whose capture mode forbids
  * allocation, and loops that cannot afford cudaMalloc's synchronisation.
- * nbf > SQ_NOALLOC_MAX_NBF is rejected with SQ_ERR_ARG.  The first call on a
- * device looks up the array's device address; make it before any stream
- * capture.  Calls share the array, so calls that overlap on the GPU race and
- * must be serialised by the caller; each FP32 call overwrites the array
- * before reading it.  Allocates nothing. */
+ * The limit is in matrix elements: nbf > SQ_NOALLOC_MAX_NBF, or a density of
+ * more than SQ_NOALLOC_MAX_ELEMS elements (mat_total of a packed batch basis,
+ * sum_i n_i^2, whatever its nbf), is rejected with SQ_ERR_ARG before any
+ * device work.  Every call looks up (first call on a device) or reuses the
+ * array's device address; make the first call on each device before any
+ * stream capture.  Calls share the array, so calls that overlap on the GPU
+ * race and must be serialised by the caller; each FP32 call overwrites the
+ * elements it reads before reading them.  Allocates nothing. */
 #define SQ_NOALLOC_MAX_NBF 1024
+#define SQ_NOALLOC_MAX_ELEMS (SQ_NOALLOC_MAX_NBF * SQ_NOALLOC_MAX_NBF)
 int sq_jk_noalloc(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, const sq_quartets *quartets,
                   const double *table64, const float *table32, const double *D, double *Jacc, double *Kacc,
                   int precision, void *stream);

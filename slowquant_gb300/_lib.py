@@ -39,6 +39,7 @@ SQ_OPT_JK_STREAMS = 2
 SQ_OPT_FP64_UNROLLED_HIGH = 3
 SQ_OPT_GRAD_THREAD = 4
 SQ_NOALLOC_MAX_NBF = 1024
+SQ_NOALLOC_MAX_ELEMS = SQ_NOALLOC_MAX_NBF * SQ_NOALLOC_MAX_NBF
 
 PRECISIONS = {"fp64": SQ_FP64, "fp32": SQ_FP32, "fp32_boys32": SQ_FP32_BOYS32}
 
@@ -80,6 +81,24 @@ class SqQuartets(ctypes.Structure):
 _lib = None
 
 
+def _preload_torch_linalg() -> None:
+    """Load torch's CUDA linear-algebra library by absolute path, once.
+
+    torch opens libtorch_cuda_linalg.so by bare name on the first torch.linalg
+    call on a CUDA tensor.  Under a profiler that interposes dlopen (ncu) that
+    name no longer resolves through torch's run path and the call fails;
+    loaded here by path with RTLD_GLOBAL, the later dlopen finds this copy.
+    """
+    try:
+        import torch
+
+        path = os.path.join(os.path.dirname(torch.__file__), "lib", "libtorch_cuda_linalg.so")
+        if os.path.exists(path):
+            ctypes.CDLL(path, mode=ctypes.RTLD_GLOBAL)
+    except OSError:
+        pass
+
+
 def lib() -> ctypes.CDLL:
     """Load libsqgb300.so (raises if it has not been built)."""
     global _lib
@@ -89,6 +108,7 @@ def lib() -> ctypes.CDLL:
                 f"{LIB_PATH} is missing: build the CUDA library first "
                 "(python -m slowquant_gb300.build); there is no CPU fallback"
             )
+        _preload_torch_linalg()
         L = ctypes.CDLL(LIB_PATH)
         L.sq_last_error.restype = ctypes.c_char_p
         L.sq_version.restype = ctypes.c_int

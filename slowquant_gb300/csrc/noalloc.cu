@@ -10,27 +10,34 @@
 // library's own device memory, reserved when the library is loaded.
 //
 // Limits and behaviour:
-//   * nbf <= SQ_NOALLOC_MAX_NBF (1024): the array holds 1024 x 1024 floats
-//     (4 MiB) on every GPU that loads the library, until the process exits;
-//     larger bases are rejected with SQ_ERR_ARG before anything is launched;
-//   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress, with that device current) and caches it; make
-//     that first call before any stream capture;
+//   * the density handed to the FP32 launches holds at most
+//     SQ_NOALLOC_MAX_ELEMS (1024 x 1024) elements: nbf <= 1024 for one
+//     molecule, and a packed batch basis (mat_base != NULL) must have
+//     mat_total = sum_i n_i^2 <= 1024 x 1024 whatever its nbf (nbf of a batch
+//     is only its largest molecule).  The array is 4 MiB on every GPU that
+//     loads the library, held until the process exits; larger inputs are
+//     rejected with SQ_ERR_ARG before anything is launched;
+//   * every call (whatever its precision) first makes sure the array's device
+//     address is known for the current device: the first call on a device
+//     looks it up (cudaGetSymbolAddress, with that device current) and caches
+//     it, so make that first call before any stream capture;
 //   * every call shares the one array: calls that overlap on the GPU (two
 //     streams, or two host threads) race on it and must be serialised by the
 //     caller.  The array keeps the last call's FP32 density; nothing in it has
-//     to start at zero because each FP32 call overwrites it in full first;
+//     to start at zero because each FP32 call overwrites its first mat_total
+//     elements before reading them;
 //   * no cudaMalloc, cudaFree or allocating library routine is called.
 #include <mutex>
 
 #include "capi_internal.cuh"
+#include "sq_common.cuh"
 
 namespace {
 
 constexpr int kMaxDevices = 64;
 
 // File-scope scratch: the FP32 copy of the density matrix.
-static __device__ __align__(256) float g_density32_scratch[SQ_NOALLOC_MAX_NBF * SQ_NOALLOC_MAX_NBF];
+static __device__ __align__(256) float g_density32_scratch[SQ_NOALLOC_MAX_ELEMS];
 
 std::mutex g_scratch_mutex;
 float *g_scratch_addr[kMaxDevices] = {nullptr};
@@ -66,12 +73,21 @@ extern "C" int sq_jk_noalloc(const sq_basis *basis, const sq_pairs *pairs, const
                              "sq_jk_noalloc: nbf = %d exceeds the static scratch limit of %d basis functions "
                              "(use sq_jk with caller-allocated scratch)",
                              basis->nbf, SQ_NOALLOC_MAX_NBF);
+    // the FP32 density covers mat_total elements: n^2 for one molecule, the
+    // packed length sum_i n_i^2 for a batch (whose nbf is its largest molecule)
+    const long long mt = sq::mat_total(*basis);
+    if (mt < 0 || mt > (long long)SQ_NOALLOC_MAX_ELEMS)
+        return sq::set_error(SQ_ERR_ARG,
+                             "sq_jk_noalloc: the density holds %lld elements, which exceeds the static scratch "
+                             "limit of %lld elements (use sq_jk with caller-allocated scratch)",
+                             mt, (long long)SQ_NOALLOC_MAX_ELEMS);
+    // resolved on every call, FP64 ones included, so that the first call on a
+    // device (whatever its precision) is the one that looks the address up
     float *d32 = nullptr;
-    if (precision != SQ_FP64) {
-        const int rc = scratch_address(&d32);
-        if (rc != SQ_OK) return rc;
-    }
+    const int rc = scratch_address(&d32);
+    if (rc != SQ_OK) return rc;
     // serial launches on the caller's stream: the library's stream pool would
     // create streams and events on its first use
-    return sq::jk_serial(basis, pairs, slots, quartets, table64, table32, D, d32, Jacc, Kacc, precision, stream);
+    return sq::jk_serial(basis, pairs, slots, quartets, table64, table32, D, precision == SQ_FP64 ? nullptr : d32, Jacc,
+                         Kacc, precision, stream);
 }

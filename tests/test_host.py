@@ -338,3 +338,35 @@ def test_abi_refuses_bad_arguments_before_touching_the_device():
     finally:
         for k, v in defaults.items():
             L.sq_set_option(k, v)
+
+
+def test_noalloc_refuses_packed_density_beyond_scratch_before_device_work():
+    """sq_jk_noalloc bounds the packed density length, not only nbf.
+
+    A batch basis (mat_base set) has nbf = its largest molecule, while its
+    matrices hold sum_i n_i^2 elements; the static FP32 scratch holds
+    SQ_NOALLOC_MAX_ELEMS.  The refusal must come back as SQ_ERR_ARG before any
+    CUDA call: no pointer below is dereferenced and no GPU is needed.
+    """
+    from slowquant_gb300 import _lib, build
+
+    if not os.path.exists(_lib.LIB_PATH):
+        build.build()
+    L = _lib.lib()
+    b = _lib.SqBasis()
+    b.nbf = 50  # small largest molecule ...
+    b.mat_base = 0x1000  # ... in a packed batch (never read: refused first)
+    b.mat_ld = 0x1000
+    b.mat_total = _lib.SQ_NOALLOC_MAX_ELEMS + 1  # ... whose matrices overflow the scratch
+    for prec in (_lib.SQ_FP32, _lib.SQ_FP64):
+        rc = L.sq_jk_noalloc(ctypes.byref(b), None, None, None, None, None, None, None, None, prec, None)
+        assert rc == _lib.SQ_ERR_ARG
+        assert b"static scratch limit" in L.sq_last_error() and b"elements" in L.sq_last_error()
+    b.mat_total = -1
+    assert L.sq_jk_noalloc(ctypes.byref(b), None, None, None, None, None, None, None, None, 1, None) == \
+        _lib.SQ_ERR_ARG
+    one = _lib.SqBasis()
+    one.nbf = _lib.SQ_NOALLOC_MAX_NBF + 1
+    assert L.sq_jk_noalloc(ctypes.byref(one), None, None, None, None, None, None, None, None, 1, None) == \
+        _lib.SQ_ERR_ARG
+    assert b"basis functions" in L.sq_last_error()
