@@ -122,7 +122,8 @@ def fma_peak(lib, torch, precision: int) -> float:
     """Measured FMA throughput (FLOP/s) of one pipe via the library's probe kernel."""
     from slowquant_gb300 import _lib
 
-    blocks, iters = 152 * 8, (20000 if precision == _lib.SQ_FP64 else 400000)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, iters = sms * 8, (20000 if precision == _lib.SQ_FP64 else 400000)
     out = torch.empty(blocks * 256, dtype=torch.float64, device="cuda")
     s = _lib.stream_handle()
     _lib.check(lib.sq_fma_probe(precision, blocks, 100, out.data_ptr(), s), "sq_fma_probe")

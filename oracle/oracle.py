@@ -203,6 +203,31 @@ class OracleMolecule:
         assert rc == 0
         return out
 
+    def jk_direct(self, D: np.ndarray, threshold: float = 1e-12, nthreads: int = 0, accurate: bool = True,
+                  cs: np.ndarray | None = None):
+        """J, K of hartreefock_in_memory.py:55-56 from the screened unique quartets, no stored tensor.
+
+        ``accurate`` evaluates the Boys function to full double precision (the
+        oracle's mode 1) instead of the reference's truncated series; the
+        Schwarz matrix ``cs`` (default: computed here) screens as the driver does.
+        """
+        L = lib()
+        L.sqo_set_boys_mode(1 if accurate else 0)
+        try:
+            if cs is None:
+                cs = self.schwarz(nthreads)
+            n = self.nbf
+            Dc = np.ascontiguousarray(D, dtype=np.float64)
+            J, K = np.zeros((n, n)), np.zeros((n, n))
+            B = self.cbasis()
+            rc = L.sqo_jk_direct(ctypes.byref(B), cs.ctypes.data_as(ctypes.c_void_p), ctypes.c_double(threshold),
+                                 Dc.ctypes.data_as(ctypes.c_void_p), J.ctypes.data_as(ctypes.c_void_p),
+                                 K.ctypes.data_as(ctypes.c_void_p), nthreads)
+            assert rc == 0
+        finally:
+            L.sqo_set_boys_mode(0)
+        return J, K
+
     def one_electron(self):
         n = self.nbf
         S, T, V = np.zeros((n, n)), np.zeros((n, n)), np.zeros((n, n))

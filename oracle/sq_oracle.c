@@ -14,6 +14,7 @@
  *   electron_repulsion_integral slowquant/molecularintegrals/electronrepulsion.py:107-297
  *   electron_repulsion_integral_driver  electronrepulsion.py:11-104
  *   get_cauchy_schwarz_matrix  electronrepulsion.py:300-339
+ *   J/K einsums (direct)       slowquant/hartreefock/hartreefock_in_memory.py:55-56
  *   multipole (overlap)        slowquant/molecularintegrals/multipole.py:48-135
  *   kinetic_energy_integral    slowquant/molecularintegrals/kineticenergy.py:42-133
  *   nuclear_attraction_integral slowquant/molecularintegrals/nuclearattraction.py:47-135
@@ -505,6 +506,120 @@ int sqo_eri_quartets(const sqo_basis *B, const int *quartets, long nq, double *o
         }
         free(work);
     }
+    return err;
+}
+
+/*
+ * Integral-direct J and K: the two einsums of hartreefock_in_memory.py:55-56,
+ *   J[p,q] = sum_rs V[p,q,r,s] D[s,r],   K[p,q] = sum_rs V[p,s,q,r] D[s,r],
+ * over the tensor that electronrepulsion.py:11-104 would store, without
+ * storing it.  The shell quartets are those of the driver (i <= j, k <= l,
+ * pair (i,j) at or after pair (k,l), Schwarz skip cs[i,j] cs[k,l] < thr),
+ * enumerated once each.  Every element of a block stands for the distinct
+ * index tuples of its 8-fold orbit (the tuples the driver's scatter writes);
+ * the element that is the lexicographically smallest member of its orbit
+ * inside this block's index ranges adds the orbit's tuples to J and K, so
+ * each tensor entry is summed exactly once, as in the einsum.  OpenMP threads
+ * accumulate into private matrices that are added at the end.  cs may be NULL.
+ */
+static int in_block(const sqo_basis *B, const int *sh, const long *t) {
+    for (int q = 0; q < 4; q++)
+        if (t[q] < B->bf_off[sh[q]] || t[q] >= B->bf_off[sh[q]] + B->ncart[sh[q]]) return 0;
+    return 1;
+}
+
+static int tuple_less(const long *a, const long *b) {
+    for (int q = 0; q < 4; q++) {
+        if (a[q] != b[q]) return a[q] < b[q];
+    }
+    return 0;
+}
+
+int sqo_jk_direct(const sqo_basis *B, const double *cs, double thr, const double *D, double *J, double *K,
+                  int nthreads) {
+    int maxL, maxprim, maxcart;
+    basis_limits(B, &maxL, &maxprim, &maxcart);
+    const int n = B->nshell;
+    const long nbf = B->nbf;
+    const size_t wsz = eri_work_size(B);
+    const size_t bsz = (size_t)maxcart * maxcart * maxcart * maxcart;
+    const long npair = (long)n * (n + 1) / 2;
+    int *pi = (int *)malloc(npair * sizeof(int)), *pj = (int *)malloc(npair * sizeof(int));
+    if (!pi || !pj) return 1;
+    long np_ = 0;
+    for (int i = 0; i < n; i++)
+        for (int j = i; j < n; j++) {
+            pi[np_] = i;
+            pj[np_] = j;
+            np_++;
+        }
+    memset(J, 0, nbf * nbf * sizeof(double));
+    memset(K, 0, nbf * nbf * sizeof(double));
+    int err = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel
+    {
+        double *work = (double *)malloc(wsz * sizeof(double));
+        double *blk = (double *)malloc(bsz * sizeof(double));
+        double *Jt = (double *)calloc(nbf * nbf, sizeof(double));
+        double *Kt = (double *)calloc(nbf * nbf, sizeof(double));
+        if (!work || !blk || !Jt || !Kt) {
+#pragma omp atomic write
+            err = 1;
+        } else {
+#pragma omp for schedule(dynamic, 1)
+            for (long P = npair - 1; P >= 0; P--) {
+                const int i = pi[P], j = pj[P];
+                for (long Q = 0; Q <= P; Q++) {
+                    const int k = pi[Q], l = pj[Q];
+                    if (cs && cs[i * n + j] * cs[k * n + l] < thr) continue;
+                    const int sh[4] = {i, j, k, l};
+                    eri_block(B, i, j, k, l, blk, work, 0);
+                    const int nb1 = B->ncart[i], nb2 = B->ncart[j], nb3 = B->ncart[k], nb4 = B->ncart[l];
+                    for (int a = 0; a < nb1; a++)
+                        for (int b = 0; b < nb2; b++)
+                            for (int c = 0; c < nb3; c++)
+                                for (int d = 0; d < nb4; d++) {
+                                    const double v = blk[((a * nb2 + b) * nb3 + c) * nb4 + d];
+                                    const long A = B->bf_off[i] + a, Bq = B->bf_off[j] + b, C = B->bf_off[k] + c,
+                                               Dd = B->bf_off[l] + d;
+                                    const long perm[8][4] = {{A, Bq, C, Dd}, {Bq, A, C, Dd}, {A, Bq, Dd, C},
+                                                             {Bq, A, Dd, C}, {C, Dd, A, Bq}, {C, Dd, Bq, A},
+                                                             {Dd, C, A, Bq}, {Dd, C, Bq, A}};
+                                    int first = 1;
+                                    for (int x = 1; x < 8 && first; x++)
+                                        if (in_block(B, sh, perm[x]) && tuple_less(perm[x], perm[0])) first = 0;
+                                    if (!first) continue;
+                                    for (int x = 0; x < 8; x++) {
+                                        int dup = 0;
+                                        for (int y = 0; y < x && !dup; y++)
+                                            dup = perm[y][0] == perm[x][0] && perm[y][1] == perm[x][1] &&
+                                                  perm[y][2] == perm[x][2] && perm[y][3] == perm[x][3];
+                                        if (dup) continue;
+                                        const long w = perm[x][0], xx = perm[x][1], y = perm[x][2], z = perm[x][3];
+                                        Jt[w * nbf + xx] += v * D[z * nbf + y];
+                                        Kt[w * nbf + y] += v * D[xx * nbf + z];
+                                    }
+                                }
+                }
+            }
+#pragma omp critical
+            {
+                for (long x = 0; x < nbf * nbf; x++) {
+                    J[x] += Jt[x];
+                    K[x] += Kt[x];
+                }
+            }
+        }
+        free(work);
+        free(blk);
+        free(Jt);
+        free(Kt);
+    }
+    free(pi);
+    free(pj);
     return err;
 }
 

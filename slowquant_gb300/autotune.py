@@ -17,7 +17,6 @@ import torch
 from . import _lib
 from .engine import QuartetList
 
-SMS = 152
 THREADS = (64, 128)
 WAVES = (1, 2, 4, 8, 16, 64, 128)
 
@@ -52,6 +51,7 @@ def reset() -> None:
 def tune(run_class, lists, precs, threads=THREADS, waves=WAVES) -> dict:
     """run_class(sub_list, prec) launches one class; lists/precs as for jk_accumulate."""
     lib = _lib.lib()
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     table = {}
     for ql, prec in zip(lists, precs):
         p = _lib.PRECISIONS[prec]
@@ -66,7 +66,7 @@ def tune(run_class, lists, precs, threads=THREADS, waves=WAVES) -> dict:
             best = (0, 0, _time(lambda: run_class(sub, prec)))
             for t in threads:
                 for w in waves:
-                    blocks = SMS * w * (128 // t)
+                    blocks = sms * w * (128 // t)
                     _lib.check(lib.sq_set_launch_config(c, p, t, blocks), "sq_set_launch_config")
                     ms = _time(lambda: run_class(sub, prec))
                     if ms < best[2]:

@@ -59,7 +59,9 @@ def parse_turbomole(path: str) -> dict[str, list[dict]]:
 
 
 def main() -> None:
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/slowquant/molecule/basisset"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python convert_basis.py <SlowQuant checkout>/slowquant/molecule/basisset")
+    src = sys.argv[1]
     for fname in sorted(os.listdir(src)):
         if not fname.endswith(".basis"):
             continue

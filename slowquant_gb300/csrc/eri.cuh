@@ -481,7 +481,7 @@ cudaError_t launch_eri_class(const EriArgs &args, int mode, int precision, cudaS
     long long blocks = (args.nq + threads - 1) / threads;
     // FP64: many blocks (FP64-bound, heavy-first order balances); FP32: about
     // two waves of persistent blocks so the shared Boys table is loaded rarely.
-    const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : (precision == SQ_FP64 ? 152LL * 16 * 8 : 152LL * 16);
+    const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : (precision == SQ_FP64 ? sm_count() * 16 * 8 : sm_count() * 16);
     if (blocks > cap) blocks = cap;
     (void)mode;  // per-thread kernels serve J/K launches only
     if (precision == SQ_FP64)
@@ -501,7 +501,7 @@ cudaError_t launch_eri_class_f64(const EriArgs &args, int mode, int precision, c
     if (args.nq <= 0) return cudaSuccess;
     const int threads = args.cfg_threads > 0 ? args.cfg_threads : 128;
     long long blocks = (args.nq + threads - 1) / threads;
-    const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : 152LL * 16 * 8;
+    const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : sm_count() * 16 * 8;
     if (blocks > cap) blocks = cap;
     eri_class_kernel<LA, LB, LC, LD, double, BOYS_FP64, MODE_JK><<<(int)blocks, threads, 0, stream>>>(args);
     return cudaGetLastError();
@@ -516,7 +516,7 @@ cudaError_t launch_eri_class_f32(const EriArgs &args, int mode, int precision, c
     if (args.nq <= 0) return cudaSuccess;
     const int threads = args.cfg_threads > 0 ? args.cfg_threads : 128;
     long long blocks = (args.nq + threads - 1) / threads;
-    const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : 152LL * 16;
+    const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : sm_count() * 16;
     if (blocks > cap) blocks = cap;
     eri_class_kernel<LA, LB, LC, LD, float, BOYS_FP64, MODE_JK><<<(int)blocks, threads, 0, stream>>>(args);
     return cudaGetLastError();

@@ -392,7 +392,7 @@ static cudaError_t launch_block(const EriArgs &args, const BlockClass &cls, cuda
     if (e != cudaSuccess) return e;
     const int threads = block_threads(cls.la, cls.lb, cls.lc, cls.ld);
     long long blocks = args.nq;
-    if (blocks > 152LL * 32) blocks = 152LL * 32;
+    if (blocks > sm_count() * 32) blocks = sm_count() * 32;
     kern<<<(unsigned)blocks, threads, lay.total, stream>>>(args, cls);
     return cudaGetLastError();
 }

@@ -422,7 +422,7 @@ inline cudaError_t launch_eri_warp(const EriArgs &args, const WarpClass &cls, in
         warp_epi_size(cls.la, cls.lb, cls.lc, cls.ld) > kWarpEpi)
         return cudaErrorInvalidValue;
     long long blocks = (args.nq + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : 152LL * 64;
+    const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : sm_count() * 64;
     if (blocks > cap) blocks = cap;
     const dim3 grid((unsigned)blocks), block(32 * kWarpsPerBlock);
 #define SQ_WARP_LAUNCH(R, B, M, K)                                                                              \

@@ -556,7 +556,7 @@ extern "C" int sq_grad_2e(const sq_basis *basis, const sq_pairs *pairs, const sq
         a.nq = nq;
         const size_t sz = (size_t)lay.stride * sizeof(double) * kGradWarps;
         long long blocks = (nq + kGradWarps - 1) / kGradWarps;
-        if (blocks > 152LL * 64) blocks = 152LL * 64;
+        if (blocks > sm_count() * 64) blocks = sm_count() * 64;
         for (int swap = 0; swap < 2; ++swap) {
             // light classes: one quartet per thread; the rest: one per warp
             if (grad_thread_enabled() &&

@@ -222,7 +222,7 @@ template <int LA, int LB, int LC, int LD>
 cudaError_t launch_grad_thread(const EriArgs &a, int swap, double *grad, cudaStream_t s) {
     if (a.nq <= 0) return cudaSuccess;
     long long blocks = (a.nq + 127) / 128;
-    if (blocks > 152LL * 16 * 8) blocks = 152LL * 16 * 8;
+    if (blocks > sm_count() * 16 * 8) blocks = sm_count() * 16 * 8;
     grad2e_thread_kernel<LA, LB, LC, LD><<<(unsigned)blocks, 128, 0, s>>>(a, swap, grad);
     return cudaGetLastError();
 }

@@ -6,6 +6,7 @@
 // d: xx xy xz yy yz zz;  f: xxx xxy xxz xyy xyz xzz yyy yyz yzz zzz.
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -79,6 +80,20 @@ __device__ __forceinline__ long long mat_index(const sq_basis &bs, int s, int a,
     const long long row = (long long)__ldg(bs.bf_off + s) + a, col = (long long)__ldg(bs.bf_off + t) + b;
     if (bs.mat_base == nullptr) return row * bs.nbf + col;
     return __ldg(bs.mat_base + s) + row * __ldg(bs.mat_ld + s) + col;
+}
+
+// Streaming multiprocessors of the current device, queried once per device;
+// grid caps of the grid-stride kernels are expressed in waves of this.
+inline long long sm_count() {
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    int n = cache[dev].load(std::memory_order_relaxed);
+    if (n <= 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return 1;
+        cache[dev].store(n, std::memory_order_relaxed);
+    }
+    return n;
 }
 
 __host__ __device__ inline long long mat_total(const sq_basis &bs) {

@@ -1,8 +1,8 @@
 """Generate the golden fixtures in this folder by running the SlowQuant reference itself.
 
 This script is test infrastructure. It imports the unmodified reference package
-(``slowquant``, pure Python + numba) from ``--reference`` (default
-``/root/reference``).  numba is not installed in the build container, so a
+(``slowquant``, pure Python + numba) from the checkout given as
+``--reference``.  numba is not installed in the build container, so a
 no-op stand-in module is registered under ``sys.modules['numba']`` before the
 import: ``jit(...)`` returns the function unchanged and the numba type objects
 are inert.  The reference arithmetic then runs as CPython floats / numpy, which
@@ -11,7 +11,7 @@ differs from numba-compiled code only at the ulp level.
 Outputs (``*.npz``, ``golden_energies.json``) are small and committed; the
 parity tests read them on machines where the reference is absent.
 
-Run:  python tests/golden/make_golden.py [--reference PATH] [--only NAME ...]
+Run:  python tests/golden/make_golden.py --reference PATH [--only NAME ...]
 """
 
 from __future__ import annotations
@@ -242,7 +242,7 @@ def boys_grid(ref_boys) -> dict:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="root of a SlowQuant checkout (the directory holding slowquant/)")
     ap.add_argument("--only", nargs="*", default=None)
     args = ap.parse_args()
     install_numba_standin()
