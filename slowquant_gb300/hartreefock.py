@@ -98,6 +98,29 @@ class DirectJK:
         return self.engine.jk_multi(Ds, self.threshold, self.precision, self.fp32_threshold)
 
 
+class SphericalJK:
+    """J/K in real solid harmonics around a Cartesian J/K callable (DirectJK):
+    D_cart = T D T^T, then J = T^T J_cart T, K = T^T K_cart T, with T the
+    (n_cartesian, n_spherical) transform of slowquant_gb300.spherical."""
+
+    def __init__(self, cartesian_jk, T: torch.Tensor):
+        self.inner = cartesian_jk
+        self.T = T
+
+    def __getattr__(self, name):  # builds, mixed, fp64_tail_diis_error, switch_to_fp64 ...
+        return getattr(self.inner, name)
+
+    def __call__(self, D: torch.Tensor):
+        Tm = self.T
+        J, K = self.inner((Tm @ D @ Tm.T).contiguous())
+        return Tm.T @ J @ Tm, Tm.T @ K @ Tm
+
+    def multi(self, Ds: torch.Tensor):
+        Tm = self.T
+        J, K = self.inner.multi((Tm @ Ds @ Tm.T).contiguous())
+        return Tm.T @ J @ Tm, Tm.T @ K @ Tm
+
+
 def run_hartree_fock(S, T, V, ERI, number_electrons: int, log, dE_threshold: float, rmsd_threshold: float,
                      max_scf_iterations: int, use_diis: bool = True):
     """Restricted Hartree-Fock (hartreefock_in_memory.py:7-94).
@@ -194,10 +217,16 @@ class _HartreeFock:
     def log(self) -> str:
         return self.logger.log
 
+    def _direct_jk(self):
+        jk = DirectJK(self.int_obj.engine, self.int_obj.cauchy_schwarz_threshold, self.precision,
+                      self.fp32_schwarz_threshold, self.fp64_tail_diis_error)
+        if getattr(self.int_obj, "spherical", False):
+            return SphericalJK(jk, self.int_obj.cart_to_sph)
+        return jk
+
     def run_restricted_hartree_fock(self) -> None:
         if self.direct_jk:
-            eri = DirectJK(self.int_obj.engine, self.int_obj.cauchy_schwarz_threshold, self.precision,
-                           self.fp32_schwarz_threshold, self.fp64_tail_diis_error)
+            eri = self._direct_jk()
             S, T, V = self.int_obj.one_electron_device()
         else:
             eri = self.int_obj.electron_repulsion_tensor
@@ -215,8 +244,7 @@ class _HartreeFock:
     def run_unrestricted_hartree_fock(self) -> None:
         """UHF (hartreefockclass.py:67-91): sets E_uhf and the alpha/beta MOs, 1-RDMs and Fock matrices."""
         if self.direct_jk:
-            eri = DirectJK(self.int_obj.engine, self.int_obj.cauchy_schwarz_threshold, self.precision,
-                           self.fp32_schwarz_threshold, self.fp64_tail_diis_error)
+            eri = self._direct_jk()
             S, T, V = self.int_obj.one_electron_device()
         else:
             eri = self.int_obj.electron_repulsion_tensor

@@ -26,8 +26,14 @@ def engine_for(mol: _Molecule) -> IntegralEngine:
 
 
 class _Integral:
-    def __init__(self, molecule_object_: _Molecule) -> None:
+    """``spherical=True`` (an option the reference does not have) returns every
+    matrix and the ERI tensor in real solid harmonics (2l+1 functions per
+    shell, ``slowquant_gb300.spherical``); the default is the reference's
+    Cartesian basis."""
+
+    def __init__(self, molecule_object_: _Molecule, spherical: bool = False) -> None:
         self.molecule_object = molecule_object_
+        self.spherical = bool(spherical)
         self.store_1e_int = True
         self.store_2e_int = True
         self.logger = _Logger()
@@ -47,11 +53,33 @@ class _Integral:
         self._cauchy_schwarz_matrix = self.engine.schwarz_matrix() if self.engine.eri_supported() else None
         self.cauchy_schwarz_threshold = 10**-12
         self._one_e_dev = None
+        self._T = None
+
+    @property
+    def number_bf(self) -> int:
+        """Basis functions of the matrices this object returns (spherical or Cartesian)."""
+        return self.cart_to_sph.shape[1] if self.spherical else self.molecule_object.number_bf
+
+    @property
+    def cart_to_sph(self):
+        """(n_cartesian, n_spherical) FP64 device matrix of the solid-harmonic transform."""
+        if self._T is None:
+            import torch
+
+            from .spherical import transform_matrix
+
+            self._T = torch.tensor(transform_matrix(self.molecule_object.shells), dtype=torch.float64,
+                                   device=self.engine.device)
+        return self._T
 
     def one_electron_device(self):
-        """(S, T, V) as FP64 device tensors."""
+        """(S, T, V) as FP64 device tensors (in solid harmonics when ``spherical``)."""
         if self._one_e_dev is None or self.force_recompute:
-            self._one_e_dev = self.engine.one_electron()
+            mats = self.engine.one_electron()
+            if self.spherical:
+                Tm = self.cart_to_sph
+                mats = tuple(Tm.T @ M @ Tm for M in mats)
+            self._one_e_dev = mats
         return self._one_e_dev
 
     def _one_e(self, idx: int) -> np.ndarray:
@@ -82,7 +110,16 @@ class _Integral:
         return self._one_e(2)
 
     def _eri(self) -> np.ndarray:
-        return self.engine.eri_dense(self.cauchy_schwarz_threshold).cpu().numpy()
+        V = self.engine.eri_dense(self.cauchy_schwarz_threshold)
+        if self.spherical:
+            import torch
+
+            Tm = self.cart_to_sph
+            V = torch.einsum("pqrs,pi->iqrs", V, Tm)
+            V = torch.einsum("iqrs,qj->ijrs", V, Tm)
+            V = torch.einsum("ijrs,rk->ijks", V, Tm)
+            V = torch.einsum("ijks,sl->ijkl", V, Tm)
+        return V.cpu().numpy()
 
     @property
     def electron_repulsion_tensor(self) -> np.ndarray:

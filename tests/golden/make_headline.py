@@ -23,7 +23,7 @@ their diagonals, tr(D J), tr(D K) and E(D) = 1/2 tr D (H + F(D)) with
 F = H + J - K/2 (one Fock build, no DIIS).
 
 Run:  python tests/golden/make_headline.py [--only headline_c2 ...] [--threads N]
-(about 20 minutes for c2 and an hour for c3 on 8 cores).
+(about 3 minutes for c2 and 16 for c3 on 8 cores).
 """
 
 from __future__ import annotations

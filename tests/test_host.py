@@ -370,3 +370,24 @@ def test_noalloc_refuses_packed_density_beyond_scratch_before_device_work():
     assert L.sq_jk_noalloc(ctypes.byref(one), None, None, None, None, None, None, None, None, 1, None) == \
         _lib.SQ_ERR_ARG
     assert b"basis functions" in L.sq_last_error()
+
+
+def test_solid_harmonic_transform_is_orthonormal_per_shell():
+    """T^T S T is the identity inside every shell (d and f included), and the
+    spherical counts are those published for cc-pVXZ (24 per water in cc-pVDZ)."""
+    from slowquant_gb300 import spherical
+
+    m = molecule._Molecule("O 0 0 0;", 0, "bohr")
+    m._set_basis_set("cc-pvtz")
+    T = spherical.transform_matrix(m.shells)
+    assert T.shape == (35, 30)
+    S = O.OracleMolecule("O 0 0 0;", "cc-pvtz", "bohr").one_electron()[0]
+    Ss = T.T @ S @ T
+    off = 0
+    for s in m.shells:
+        n = 2 * int(np.sum(s.angular_moments[0])) + 1
+        np.testing.assert_allclose(Ss[off:off + n, off:off + n], np.eye(n), atol=1e-13)
+        off += n
+    w = molecule._Molecule(systems.water_cluster(16, 11.0, seed=16), 0, "angstrom")
+    w._set_basis_set("cc-pvdz")
+    assert spherical.n_spherical(w.shells) == 384 and w.number_bf == 400
