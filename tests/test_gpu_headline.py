@@ -1,0 +1,120 @@
+"""The two headline water clusters against the oracle.
+
+(H2O)_8 and (H2O)_16 in cc-pVDZ (200 and 400 Cartesian basis functions, the
+configurations the benchmark is quoted on) are far too large for the
+reference's pure-Python path, so the comparison is with the oracle's C
+restatement (tests/golden/make_headline.py wrote the fixtures): its direct
+J/K reproduces the einsums of hartreefock_in_memory.py:55-56 over the
+screened tensor of electronrepulsion.py:11-104, and its SCF loop follows
+hartreefock_in_memory.py:7-94 with the DIIS of diis.py:4-66.
+
+Checked here:
+* the FP64 SCF energy of both clusters (1e-8 Eh);
+* J and K at the oracle's converged density, through size-independent
+  projections J @ R, K @ R onto 8 seeded random vectors (1e-9: each is a sum of
+  nbf terms whose elements agree to ~1e-11), their diagonals (1e-10) and the
+  one-build energy E(D) = 1/2 tr D (H + F(D)) (1e-8 Eh);
+* the energy error of the mixed-precision builds against the oracle at the
+  bounds 1e-3, 1e-4 and 1e-5 (one build at the converged density: <= 1e-6 Eh),
+  and of a mixed SCF, which finishes in FP64 (<= 1e-8 Eh).
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+from tests.conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+SCREEN = 1e-12
+
+
+def _fixture(name):
+    path = os.path.join(GOLDEN, name + ".npz")
+    if not os.path.exists(path):
+        pytest.fail(f"missing oracle fixture {path} (tests/golden/make_headline.py)")
+    return np.load(path)
+
+
+_cache = {}
+
+
+def _setup(name):
+    if name in _cache:
+        return _cache[name]
+    import torch
+
+    from slowquant_gb300.engine import IntegralEngine
+    from slowquant_gb300.molecule import _Molecule
+
+    g = _fixture(name)
+    mol = _Molecule(str(g["geometry"]), 0, "angstrom")
+    mol._set_basis_set("cc-pvdz")
+    eng = IntegralEngine(mol)
+    assert eng.nbf == int(g["nbf"])
+    assert abs(mol.nuclear_repulsion - float(g["E_nuc"])) < 1e-9
+    S, T, V = eng.one_electron()
+    C = torch.tensor(g["C_occ"], dtype=torch.float64, device="cuda")
+    D = 2 * C @ C.T
+    R = np.random.default_rng(1234).standard_normal((eng.nbf, 8))
+    _cache[name] = (g, mol, eng, S, T, V, D, R)
+    return _cache[name]
+
+
+def _energy_at(eng, H, D, precision, tau=1e-4):
+    import torch
+
+    F = eng.fock(H, D, SCREEN, precision, tau)
+    return float(0.5 * torch.sum(D * (H + F)))
+
+
+@pytest.mark.parametrize("name", ["headline_c2", "headline_c3"])
+def test_fp64_jk_at_oracle_density(gpu_lib, name):
+    g, mol, eng, S, T, V, D, R = _setup(name)
+    J, K = eng.jk(D, SCREEN, "fp64")
+    J, K = J.cpu().numpy(), K.cpu().numpy()
+    np.testing.assert_allclose(J @ R, g["JR"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(K @ R, g["KR"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(np.diag(J), g["J_diag"], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(np.diag(K), g["K_diag"], rtol=0, atol=1e-10)
+    Dn = D.cpu().numpy()
+    assert abs(np.sum(Dn * J) - float(g["trDJ"])) < 1e-8
+    assert abs(np.sum(Dn * K) - float(g["trDK"])) < 1e-8
+    assert abs(_energy_at(eng, T + V, D, "fp64") - float(g["E_at_D"])) < 1e-8
+
+
+@pytest.mark.parametrize("name", ["headline_c2", "headline_c3"])
+def test_fp64_scf_energy_matches_oracle(gpu_lib, name):
+    from slowquant_gb300.hartreefock import DirectJK, run_hartree_fock
+    from slowquant_gb300.logger import _Logger
+
+    g, mol, eng, S, T, V, D, R = _setup(name)
+    log = _Logger()
+    log.print_output = False
+    E, _, _, _ = run_hartree_fock(S, T, V, DirectJK(eng, SCREEN, "fp64"), mol.number_electrons, log, 1e-9, 1e-9,
+                                  100, True)
+    assert abs(E - float(g["E_hf"])) < 1e-8, E - float(g["E_hf"])
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed_prim"])
+@pytest.mark.parametrize("tau", [1e-3, 1e-4, 1e-5])
+def test_mixed_one_build_energy_error_vs_oracle(gpu_lib, precision, tau):
+    g, mol, eng, S, T, V, D, R = _setup("headline_c3")
+    dE = _energy_at(eng, T + V, D, precision, tau) - float(g["E_at_D"])
+    assert abs(dE) <= 1e-6, (precision, tau, dE)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed_prim"])
+def test_mixed_scf_energy_vs_oracle(gpu_lib, precision):
+    from slowquant_gb300.hartreefock import DirectJK, run_hartree_fock
+    from slowquant_gb300.logger import _Logger
+
+    g, mol, eng, S, T, V, D, R = _setup("headline_c3")
+    log = _Logger()
+    log.print_output = False
+    jk = DirectJK(eng, SCREEN, precision, 1e-4, 1e-5)
+    E, _, _, _ = run_hartree_fock(S, T, V, jk, mol.number_electrons, log, 1e-9, 1e-9, 100, True)
+    assert jk.builds[0] == precision and jk.builds[-1] == "fp64"
+    assert abs(E - float(g["E_hf"])) < 1e-8, E - float(g["E_hf"])

@@ -391,3 +391,15 @@ def test_solid_harmonic_transform_is_orthonormal_per_shell():
     w = molecule._Molecule(systems.water_cluster(16, 11.0, seed=16), 0, "angstrom")
     w._set_basis_set("cc-pvdz")
     assert spherical.n_spherical(w.shells) == 384 and w.number_bf == 400
+
+
+def test_headline_fixtures_match_the_synthetic_generators():
+    """The oracle fixtures of the two headline clusters were made from the same seeded geometries."""
+    for name, (nw, box, seed, nbf) in {"headline_c2": (8, 9.0, 8, 200), "headline_c3": (16, 11.0, 16, 400)}.items():
+        g = np.load(os.path.join(ROOT, "tests", "golden", name + ".npz"))
+        assert str(g["geometry"]) == systems.water_cluster(nw, box, seed)
+        assert int(g["nbf"]) == nbf and g["C_occ"].shape == (nbf, 5 * nw)
+        assert g["JR"].shape == (nbf, 8) and float(g["screen"]) == 1e-12
+        # the SCF converged: the last two iteration energies agree to the SCF threshold
+        assert abs(g["energies"][-1] - g["energies"][-2]) < 1e-9
+        assert abs(float(g["E_at_D"]) - float(g["E_hf"])) < 1e-9
