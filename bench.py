@@ -42,6 +42,18 @@ def workload_geometry() -> str:
     return systems.water_cluster(WATERS, BOXES.get(WATERS, BOX), SEED)
 
 
+def oracle_fixture():
+    """The oracle's SCF fixture for the configured cluster (tests/golden/make_headline.py), or None."""
+    name = {(16, "cc-pvdz"): "headline_c3", (8, "cc-pvdz"): "headline_c2"}.get((WATERS, BASIS))
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", f"{name}.npz")
+    if name is None or not os.path.exists(path):
+        return None
+    g = np.load(path)
+    if str(g["geometry"]) != workload_geometry():
+        return None
+    return {"E_hf": float(g["E_hf"]), "E_at_D": float(g["E_at_D"])}
+
+
 def config(extra=None) -> dict:
     nbf_w, label = BASES[BASIS]
     c = {
@@ -390,6 +402,7 @@ def gpu_arm(args) -> None:
     ms_e2e = time_events(torch, step_e2e, args.steps, flush)
     e2e_ms = float(np.mean(ms_e2e))
 
+    orc = oracle_fixture()
     # precision threshold sweep: build time, one-build energy error at the FP64
     # density, and the SCF energy error (mixed SCF switches to FP64 at the end)
     Ffp = eng.fock(H, D, SCREEN, "fp64")
@@ -404,6 +417,7 @@ def gpu_arm(args) -> None:
         Et, _, _, _ = run_hartree_fock(S, T, V, jkt, ne, log, 1e-9, 1e-9, 100, True)
         sweep.append({"fp32_threshold": tau, "fock_build_ms": ms_tau, "speedup_vs_fp64": ms64 / ms_tau,
                       "dE_one_build": dE_build, "dE_scf": Et - E64,
+                      "dE_scf_vs_oracle": None if orc is None else Et - orc["E_hf"],
                       "mixed_builds": sum(1 for b in jkt.builds if b != "fp64"), "builds": len(jkt.builds)})
 
     # primitive-chunk granularity of the same precision test (beside the headline)
@@ -418,6 +432,25 @@ def gpu_arm(args) -> None:
         chunk_modes.append({"fp32_threshold": tau, "fock_build_ms": ms_c, "speedup_vs_fp64": ms64 / ms_c,
                             "dE_one_build": float(0.5 * torch.sum(D * (H + Fc))) - E_build64, "dE_scf": Ec - E64,
                             "fp64_entries": c64.nquartet, "fp32_entries": c32.nquartet})
+
+    # primitive-level precision inside the FP64 launches (sq_jk_prim) at the same bounds
+    prim_modes = []
+    for tau in args.prim_sweep:
+        eng.fock(H, D, SCREEN, "mixed_prim", tau)
+        ms_p = float(np.median(time_events(torch, lambda: eng.fock(H, D, SCREEN, "mixed_prim", tau), 5, flush)))
+        Fp = eng.fock(H, D, SCREEN, "mixed_prim", tau)
+        jkp = DirectJK(eng, SCREEN, "mixed_prim", tau, 1e-5)
+        Ep, _, _, _ = run_hartree_fock(S, T, V, jkp, ne, log, 1e-9, 1e-9, 100, True)
+        p64, p32 = eng.quartets(SCREEN, tau)
+        eng.jk_accumulate(D, [p64], ["fp64_prim"], prim_tau=tau)
+        ms_p64 = float(np.median(time_events(
+            torch, lambda: eng.jk_accumulate(D, [p64], ["fp64_prim"], prim_tau=tau), 5, flush)))
+        prim_modes.append({"fp32_threshold": tau, "fock_build_ms": ms_p, "speedup_vs_fp64": ms64 / ms_p,
+                           "dE_one_build": float(0.5 * torch.sum(D * (H + Fp))) - E_build64, "dE_scf": Ep - E64,
+                           "dE_scf_vs_oracle": None if orc is None else Ep - orc["E_hf"],
+                           "fp64_list_alone_ms": ms_p64, "fp64_list_quartets": p64.nquartet,
+                           "fp32_list_quartets": p32.nquartet,
+                           "mixed_builds": sum(1 for b in jkp.builds if b != "fp64"), "builds": len(jkp.builds)})
 
     # the two halves of the mixed build, each timed alone (all its classes, stream pool)
     ms_part = {}
@@ -461,6 +494,10 @@ def gpu_arm(args) -> None:
                           "mixed_fp64_list_alone": ms_part["fp64_list"], "mixed_fp32_list_alone": ms_part["fp32_list"]},
         "quartets_per_s": {"mixed": nq / (ms_step * 1e-3), "fp64": nq / (ms64 * 1e-3)},
         "energy": {"E_hf_fp64": E64, "E_hf_mixed": Em, "abs_dE_mixed_vs_fp64": abs(Em - E64),
+                   "E_hf_oracle": None if orc is None else orc["E_hf"],
+                   "dE_fp64_vs_oracle": None if orc is None else E64 - orc["E_hf"],
+                   "dE_mixed_vs_oracle": None if orc is None else Em - orc["E_hf"],
+                   "oracle": "tests/golden/make_headline.py: the oracle's direct J/K and SCF, FP64, accurate Boys",
                    "mixed_builds": n_mixed_builds, "total_builds_mixed": len(jkm.builds),
                    "scf_iterations_fp64": len(jk64.builds), "scf_s_fp64": round(scf64_s, 2),
                    "scf_s_mixed": round(scfm_s, 2)},
@@ -477,7 +514,9 @@ def gpu_arm(args) -> None:
                                 "peak_tflops": peak64 / 1e12, "frac": fl64 / (ms64 * 1e-3) / peak64},
         "tau_sweep": sweep,
         "chunk_precision": chunk_modes,
+        "prim_precision": prim_modes,
         "kernels_by_time": rows[:8],
+        "fp32_kernels_by_time": [r for r in rows if r["precision"] == "fp32"][:8],
         "gpu_launches": launches * args.steps,
         "clocks": clocks,
         "setup_s": round(setup_s, 2),
@@ -644,6 +683,8 @@ def main() -> None:
     ap.add_argument("--jk-streams", type=int, default=0, help="J/K class launch streams (0: library default)")
     ap.add_argument("--tau-sweep", type=float, nargs="*", default=[1e-5, 1e-4, 1e-3, 1e-2, 1e-1],
                     help="FP32 Schwarz thresholds reported beside the headline (empty: skip)")
+    ap.add_argument("--prim-sweep", type=float, nargs="*", default=[1e-4, 1e-3, 1e-2],
+                    help="bounds of the primitive-level precision mode reported beside the headline (empty: skip)")
     args = ap.parse_args()
     global WATERS, SEED, BASIS
     WATERS = SEED = args.waters

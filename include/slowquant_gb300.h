@@ -59,6 +59,8 @@ extern "C" {
 #define SQ_FP64 0             /* all arithmetic in FP64 */
 #define SQ_FP32 1             /* FP32 integral arithmetic, Boys downward recursion in FP64 */
 #define SQ_FP32_BOYS32 2      /* FP32 integral arithmetic and FP32 Boys function */
+#define SQ_FP64_PRIM 3        /* FP64 with primitive-level precision (sq_jk_prim only): primitive
+                                 quartets with q_ij q_kl below a bound run as in SQ_FP32 */
 
 /* Contracted Cartesian Gaussian shells of one molecule (device arrays).
  * Replaces the per-shell Python objects of slowquant/molecule/moleculeclass.py:269-301. */
@@ -104,6 +106,8 @@ typedef struct sq_pairs {
     double *herm;              /* Hermite-expanded E^{ab}_{tuv}, x per-component normalisation */
     float *prim32;             /* optional FP32 copy of prim (NULL: not written) */
     float *herm32;             /* optional FP32 copy of herm */
+    const double *pq;          /* optional [nprimpair] Schwarz factor sqrt((ij|ij)) of every primitive
+                                  pair (NULL: unknown); sq_slots_fill copies it into prim32v */
 } sq_pairs;
 
 /* Slot layout of the pair data for the J/K kernels.  Pairs are renumbered in
@@ -141,6 +145,24 @@ typedef struct sq_slots {
      * are linear in the integrals, so the partial quartets add up to the whole.
      * Dense-tensor, Schwarz and gradient lists must name whole slots. */
     const int *sub;
+    /* Per-slot descriptor read by the per-thread J/K kernels (required by
+     * sq_jk / sq_jk_multi / sq_jk_prim / sq_jk_noalloc; written by
+     * sq_slots_describe for all nslot slots): desc[8 s + 0..7] = npp, pbase,
+     * pstride, hbase (below 2^31), first basis function of the pair's shell a
+     * and of shell b (local to the slot's molecule), pair index with bit 30
+     * set when a == b, and the leading dimension of the molecule's n x n
+     * matrices.  Two 16-byte loads per slot replace the chain
+     * slot -> pair -> shells -> offsets. */
+    int *desc;
+    /* [nslot] offset of the slot molecule's matrix block in a packed batch,
+     * written by sq_slots_describe from basis->mat_base (NULL for one
+     * molecule: offset 0). */
+    long long *mbase;
+    /* Packed FP32 primitive data of the per-thread FP32 J/K kernels (required
+     * for FP32 launches; written by sq_slots_fill): 8 floats per primitive
+     * pair at prim32v[8 (pbase + k pstride) + f], f = p, Px, Py, Pz, U, the
+     * primitive Schwarz factor (0 when pairs->pq is NULL), 0, 0. */
+    float *prim32v;
 } sq_slots;
 
 /* Shell-quartet work list: device array of (bra pair, ket pair) index pairs,
@@ -224,6 +246,10 @@ int sq_schwarz(const sq_basis *basis, const sq_pairs *pairs, const sq_quartets *
  * electronrepulsion.py:206-237). */
 int sq_slots_fill(const sq_basis *basis, const sq_pairs *pairs, sq_slots *slots, void *stream);
 
+/* Fill slots->desc (and slots->mbase for a packed batch basis) for all
+ * nslot slots, sub-slots included.  No counterpart in the reference. */
+int sq_slots_describe(const sq_basis *basis, const sq_pairs *pairs, sq_slots *slots, void *stream);
+
 /* Dense ERI tensor V[nbf^4] (C order) from the quartets of `quartets` (slot
  * ids when slots != NULL, else pair ids), each block scattered to its eight
  * index permutations: the output of electron_repulsion_integral_driver
@@ -254,6 +280,19 @@ int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, c
 int sq_jk_multi(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, const sq_quartets *quartets,
                 const double *table64, const float *table32, int nd, const double *D, float *D32, double *Jacc,
                 double *Kacc, int precision, void *stream);
+
+/* Primitive-level precision for the large-bound quartets of a mixed build
+ * (no counterpart in the reference).  Like sq_jk with SQ_FP64, except that in
+ * the classes with per-thread kernels (la+lb+lc+ld <= 4 except (dd|ss), and
+ * (fs|ss), (fs|ps), (fp|ss)) every primitive quartet whose primitive Schwarz
+ * bound q_ij q_kl is below prim_tau is evaluated in FP32 with the FP64 Boys
+ * recursion, summed in FP32 per bra primitive pair and added into the FP64
+ * block before the FP64 digestion.  q comes from slots->prim32v (written by
+ * sq_slots_fill from pairs->pq, which must be set); FP32 slot data, herm32
+ * and table32 are required.  The other classes run plain FP64. */
+int sq_jk_prim(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, const sq_quartets *quartets,
+               const double *table64, const float *table32, const double *D, double *Jacc, double *Kacc,
+               double prim_tau, void *stream);
 
 /* J/K build for callers that cannot allocate device memory.  No counterpart
  * in the reference (it has no device code).  Same arguments and results as

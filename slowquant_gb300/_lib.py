@@ -34,6 +34,7 @@ SQ_BOYS_TAB32_SIZE = SQ_BOYS_NGRID * SQ_BOYS_NCOL + 16 * SQ_BOYS_NGRID * 4
 SQ_FP64 = 0
 SQ_FP32 = 1
 SQ_FP32_BOYS32 = 2
+SQ_FP64_PRIM = 3
 SQ_OPT_GENERIC_MIN_L = 1
 SQ_OPT_JK_STREAMS = 2
 SQ_OPT_FP64_UNROLLED_HIGH = 3
@@ -41,7 +42,7 @@ SQ_OPT_GRAD_THREAD = 4
 SQ_NOALLOC_MAX_NBF = 1024
 SQ_NOALLOC_MAX_ELEMS = SQ_NOALLOC_MAX_NBF * SQ_NOALLOC_MAX_NBF
 
-PRECISIONS = {"fp64": SQ_FP64, "fp32": SQ_FP32, "fp32_boys32": SQ_FP32_BOYS32}
+PRECISIONS = {"fp64": SQ_FP64, "fp32": SQ_FP32, "fp32_boys32": SQ_FP32_BOYS32, "fp64_prim": SQ_FP64_PRIM}
 
 _p = ctypes.c_void_p
 
@@ -58,7 +59,7 @@ class SqBasis(ctypes.Structure):
 class SqPairs(ctypes.Structure):
     _fields_ = [
         ("npair", ctypes.c_int), ("nprimpair", ctypes.c_int), ("shells", _p), ("pp_off", _p),
-        ("herm_off", _p), ("prim", _p), ("herm", _p), ("prim32", _p), ("herm32", _p),
+        ("herm_off", _p), ("prim", _p), ("herm", _p), ("prim32", _p), ("herm32", _p), ("pq", _p),
     ]
 
 
@@ -67,7 +68,7 @@ class SqSlots(ctypes.Structure):
         ("nslot", ctypes.c_int), ("npp_total", ctypes.c_longlong), ("nherm_total", ctypes.c_longlong),
         ("pair", _p), ("npp", _p), ("pbase", _p), ("pstride", _p), ("hbase", _p),
         ("prim", _p), ("herm", _p), ("prim32", _p), ("herm32", _p),
-        ("prim_src", _p), ("prim_src_off", _p), ("sub", _p),
+        ("prim_src", _p), ("prim_src_off", _p), ("sub", _p), ("desc", _p), ("mbase", _p), ("prim32v", _p),
     ]
 
 
@@ -128,9 +129,13 @@ def lib() -> ctypes.CDLL:
         L.sq_jk_multi.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
                                   ctypes.POINTER(SqQuartets), _p, _p, ctypes.c_int, _p, _p, _p, _p, ctypes.c_int, _p]
         L.sq_slots_fill.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots), _p]
+        L.sq_slots_describe.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
+                                        _p]
         L.sq_grad_2e.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
                                  ctypes.POINTER(SqQuartets), _p, _p, _p, _p]
         L.sq_grad_1e.argtypes = [ctypes.POINTER(SqBasis), _p, _p, _p, _p, _p]
+        L.sq_jk_prim.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
+                                 ctypes.POINTER(SqQuartets), _p, _p, _p, _p, _p, ctypes.c_double, _p]
         L.sq_jk_noalloc.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
                                     ctypes.POINTER(SqQuartets), _p, _p, _p, _p, _p, ctypes.c_int, _p]
         L.sq_fock_build.argtypes = [ctypes.c_int, _p, _p, _p, _p, _p, _p, _p]
@@ -146,7 +151,7 @@ def lib() -> ctypes.CDLL:
 EXPORTED = [
     "sq_version", "sq_last_error", "sq_set_option", "sq_get_option", "sq_set_launch_config", "sq_boys_table", "sq_boys",
     "sq_pair_prep", "sq_schwarz", "sq_eri_dense", "sq_jk", "sq_fock_build", "sq_one_electron",
-    "sq_quartets_expand", "sq_fma_probe", "sq_slots_fill", "sq_jk_noalloc", "sq_grad_2e", "sq_grad_1e",
+    "sq_quartets_expand", "sq_fma_probe", "sq_slots_fill", "sq_slots_describe", "sq_jk_prim", "sq_jk_noalloc", "sq_grad_2e", "sq_grad_1e",
     "sq_batched_eigh", "sq_jk_multi",
 ]
 

@@ -246,6 +246,9 @@ class BatchEngine:
             torch.empty(5 * poff, dtype=torch.float32, device=dev) if self.fp32 else None,
             torch.empty(max(hoff, 1), dtype=torch.float32, device=dev) if self.fp32 else None,
             torch.tensor(sub, **i32),
+            torch.empty(8 * len(slot_pair), **i32),  # descriptors
+            torch.empty(len(slot_pair), dtype=torch.int64, device=dev),  # matrix block offsets
+            torch.empty(max(8 * poff, 1), dtype=torch.float32, device=dev) if self.fp32 else None,
         ]
         t = self.t_slot
         s = SqSlots()
@@ -253,11 +256,14 @@ class BatchEngine:
         s.pair, s.npp, s.pbase, s.pstride, s.hbase = ptr(t[0]), ptr(t[1]), ptr(t[2]), ptr(t[3]), ptr(t[4])
         s.prim, s.herm, s.prim32, s.herm32 = ptr(t[5]), ptr(t[6]), ptr(t[7]), ptr(t[8])
         s.sub = ptr(t[9])
+        s.desc, s.mbase, s.prim32v = ptr(t[10]), ptr(t[11]), ptr(t[12])
         self.slots = s
         fill = SqSlots.from_buffer_copy(s)
         fill.nslot = nslot  # the parents' data only: sub-slots point into it
         check(self.lib.sq_slots_fill(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(fill),
                                      self._stream()), "sq_slots_fill")
+        check(self.lib.sq_slots_describe(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(s),
+                                         self._stream()), "sq_slots_describe")
 
     # ---------------------------------------------------------- quartets
     def quartets(self, threshold: float, fp32_threshold: float | None = None):

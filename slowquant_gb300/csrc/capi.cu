@@ -166,9 +166,10 @@ static cudaError_t launch_class(EriArgs &args, const sq_quartets *qs, int c, int
     args.nq = qs->class_off[c + 1] - qs->class_off[c];
     int la, lb, lc, ld;
     quartet_class_l(c, la, lb, lc, ld);
-    if (mode == MODE_JK && precision >= 0 && precision < 3) {
-        args.cfg_threads = g_cfg[c][precision].threads;
-        args.cfg_blocks = g_cfg[c][precision].blocks;
+    if (mode == MODE_JK && precision >= 0 && precision <= SQ_FP64_PRIM) {
+        const int pi = precision == SQ_FP64_PRIM ? SQ_FP64 : precision;
+        args.cfg_threads = g_cfg[c][pi].threads;
+        args.cfg_blocks = g_cfg[c][pi].blocks;
     } else {
         args.cfg_threads = 0;
         args.cfg_blocks = 0;
@@ -180,12 +181,17 @@ static cudaError_t launch_class(EriArgs &args, const sq_quartets *qs, int c, int
     if (mode == MODE_JK && L < g_generic_min_l) unrolled = kLaunchers[c];
     if (mode == MODE_JK && precision == SQ_FP32 && kLaunchersF32[c] != nullptr && g_generic_min_l > 0)
         unrolled = kLaunchersF32[c];
-    if (mode == MODE_JK && precision == SQ_FP64 && kLaunchersF64[c] != nullptr && g_generic_min_l > 0 &&
-        ((g_fp64_unrolled_high >> c) & 1))
+    if (mode == MODE_JK && (precision == SQ_FP64 || precision == SQ_FP64_PRIM) && kLaunchersF64[c] != nullptr &&
+        g_generic_min_l > 0 && ((g_fp64_unrolled_high >> c) & 1))
         unrolled = kLaunchersF64[c];
-    if (unrolled != nullptr) return unrolled(args, mode, precision, stream);
-    if (!warp_fits) return launch_eri_block(args, la, lb, lc, ld, mode, precision, stream);
-    return launch_eri_warp(args, WarpClass{la, lb, lc, ld}, mode, precision, stream);
+    // SQ_FP64_PRIM reaches only the per-thread kernels of kLaunchers; every
+    // other kernel runs such a launch as plain FP64
+    const int plain = precision == SQ_FP64_PRIM ? SQ_FP64 : precision;
+    if (mode == MODE_JK && precision == SQ_FP64_PRIM && L < g_generic_min_l && kLaunchers[c] != nullptr)
+        return kLaunchers[c](args, mode, precision, stream);
+    if (unrolled != nullptr) return unrolled(args, mode, plain, stream);
+    if (!warp_fits) return launch_eri_block(args, la, lb, lc, ld, mode, plain, stream);
+    return launch_eri_warp(args, WarpClass{la, lb, lc, ld}, mode, plain, stream);
 }
 
 static int run_classes(const char *who, EriArgs args, const sq_quartets *qs, int mode, int precision,
@@ -316,19 +322,28 @@ extern "C" int sq_eri_dense(const sq_basis *basis, const sq_pairs *pairs, const 
 static int jk_common(const char *who, const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots,
                      const sq_quartets *quartets, const double *table64, const float *table32, int nd,
                      const double *D, float *D32, double *Jacc, double *Kacc, int precision, void *stream,
-                     bool pooled = true) {
+                     bool pooled = true, float prim_tau = 0.0f) {
     int rc = check_common(who, basis, pairs, quartets, table64);
     if (rc) return rc;
-    if (!slots || !slots->prim || !slots->herm || !slots->pair)
-        return set_error(SQ_ERR_ARG, "%s: slot layout is required", who);
+    if (!slots || !slots->prim || !slots->herm || !slots->pair || !slots->desc)
+        return set_error(SQ_ERR_ARG, "%s: slot layout with descriptors (sq_slots_describe) is required", who);
+    if (basis->mat_base != nullptr && !slots->mbase)
+        return set_error(SQ_ERR_ARG, "%s: a packed batch basis needs slots->mbase", who);
     if (!D || !Jacc || !Kacc) return set_error(SQ_ERR_ARG, "%s: D, Jacc and Kacc are required", who);
     if (nd < 1) return set_error(SQ_ERR_ARG, "%s: nd = %d densities", who, nd);
-    if (precision != SQ_FP64 && precision != SQ_FP32 && precision != SQ_FP32_BOYS32)
+    if (precision != SQ_FP64 && precision != SQ_FP32 && precision != SQ_FP32_BOYS32 && precision != SQ_FP64_PRIM)
         return set_error(SQ_ERR_ARG, "%s: unknown precision %d", who, precision);
+    if (precision == SQ_FP64_PRIM &&
+        (!pairs->pq || !slots->prim32v || !slots->herm32 || !table32 || !(prim_tau >= 0.0f)))
+        return set_error(SQ_ERR_ARG, "%s: primitive-level precision needs pairs->pq, FP32 slot data, table32 and a "
+                         "non-negative bound", who);
     cudaStream_t s = (cudaStream_t)stream;
     const long long mt = mat_total(*basis);
-    if (precision != SQ_FP64) {
-        if (!D32 || !pairs->prim32 || !pairs->herm32 || !slots->prim32 || !slots->herm32 || !table32)
+    if (mt >= (1LL << 31))
+        return set_error(SQ_ERR_ARG, "%s: %lld matrix elements exceed the kernels' 32-bit indexing", who, mt);
+    if (precision != SQ_FP64 && precision != SQ_FP64_PRIM) {
+        if (!D32 || !pairs->prim32 || !pairs->herm32 || !slots->prim32 || !slots->herm32 || !slots->prim32v ||
+            !table32)
             return set_error(SQ_ERR_ARG, "%s: FP32 precision needs D32, FP32 pair/slot data and table32", who);
         rc = to_float(mt * nd, D, D32, s);
         if (rc) return rc;
@@ -346,6 +361,7 @@ static int jk_common(const char *who, const sq_basis *basis, const sq_pairs *pai
     a.use_slots = 1;
     a.Jacc = Jacc;
     a.Kacc = Kacc;
+    a.prim_tau = prim_tau;
     return run_classes(who, a, quartets, MODE_JK, precision, s, pooled);
 }
 
@@ -363,6 +379,13 @@ extern "C" int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_slot
                      float *D32, double *Jacc, double *Kacc, int precision, void *stream) {
     return jk_common("sq_jk", basis, pairs, slots, quartets, table64, table32, 1, D, D32, Jacc, Kacc, precision,
                      stream);
+}
+
+extern "C" int sq_jk_prim(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots,
+                          const sq_quartets *quartets, const double *table64, const float *table32, const double *D,
+                          double *Jacc, double *Kacc, double prim_tau, void *stream) {
+    return jk_common("sq_jk_prim", basis, pairs, slots, quartets, table64, table32, 1, D, nullptr, Jacc, Kacc,
+                     SQ_FP64_PRIM, stream, true, (float)prim_tau);
 }
 
 extern "C" int sq_jk_multi(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots,

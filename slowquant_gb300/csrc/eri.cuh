@@ -50,6 +50,7 @@ struct EriArgs {
     long long cfg_blocks;
     int nd;                 // J/K: densities digested per integral (0 or 1: one)
     long long dstride;      // elements between consecutive densities / accumulators
+    float prim_tau;         // SQ_FP64_PRIM launches: primitive quartets with q_ij q_kl < prim_tau run in FP32
 };
 
 constexpr double kTwoPi52 = 34.98683665524972;  // 2 pi^{5/2}
@@ -142,164 +143,467 @@ __device__ __forceinline__ T gload(const T *p) {
     return __ldg(p);
 }
 
+// Per-slot descriptor (sq_slots::desc): primitive-pair layout of the slot and
+// what the J/K epilogue needs to index the n x n matrices.
+struct SlotDesc {
+    int npp, pbase, pstride, hbase;
+    int oa, ob;   // first basis function of shells a, b (molecule-local)
+    int pairf;    // pair index, bit 30 set when a == b
+    int ld;       // leading dimension of the molecule's matrices
+};
+
+__device__ __forceinline__ SlotDesc load_desc(const int *desc, int s) {
+    const int4 *d = reinterpret_cast<const int4 *>(desc) + 2 * (long long)s;
+    const int4 x = __ldg(d), y = __ldg(d + 1);
+    return SlotDesc{x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
+}
+
+// The primitive half of a descriptor and, separately, its epilogue half (oa,
+// ob, pairf, ld), for kernels that load the latter only after the primitive
+// loops to keep it out of their registers.
+__device__ __forceinline__ SlotDesc load_desc_prims(const int *desc, int s) {
+    const int4 x = __ldg(reinterpret_cast<const int4 *>(desc) + 2 * (long long)s);
+    return SlotDesc{x.x, x.y, x.z, x.w, 0, 0, 0, 0};
+}
+
+__device__ __forceinline__ void load_desc_epilogue(const int *desc, int s, SlotDesc &d) {
+    const int4 y = __ldg(reinterpret_cast<const int4 *>(desc) + 2 * (long long)s + 1);
+    d.oa = y.x;
+    d.ob = y.y;
+    d.pairf = y.z;
+    d.ld = y.w;
+}
+
+// Fields of one primitive pair of the slot layout: exponent sum, centre, U.
+template <typename R>
+struct PrimPair {
+    R p, x, y, z, u;
+};
+
+// FP64 reads the field-major arrays (five coalesced loads), FP32 the packed
+// copy (one 16-byte load plus one 4-byte load).
+template <typename R>
+__device__ __forceinline__ PrimPair<R> load_prim(const sq_slots &sl, long long idx) {
+    if constexpr (std::is_same<R, double>::value) {
+        const long long NPP = sl.npp_total;
+        return PrimPair<R>{__ldg(sl.prim + idx), __ldg(sl.prim + NPP + idx), __ldg(sl.prim + 2 * NPP + idx),
+                           __ldg(sl.prim + 3 * NPP + idx), __ldg(sl.prim + 4 * NPP + idx)};
+    } else {
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(sl.prim32v) + 2 * idx);
+        return PrimPair<R>{a.x, a.y, a.z, a.w, __ldg(sl.prim32v + 8 * idx + 4)};
+    }
+}
+
+// W[tuv][cd] of one bra primitive pair (exponent sum p, centre P) summed
+// over the ket primitive pairs k0 <= k < k1 of slot kd, in precision R:
+//   W[tuv][cd] += sum_k U_k / sqrt(p+q) sum_{tau nu phi} (-1)^{tau+nu+phi} E^{cd}_{tau nu phi}(k) R_{t+tau,u+nu,v+phi}
+template <int LA, int LB, int LC, int LD, typename R, int BOYS>
+__device__ __forceinline__ void ket_loop(const EriArgs &args, R p, R Px, R Py, R Pz, const SlotDesc &kd, int k0, int k1,
+                                         const float4 *tb0, const float4 *tb1,
+                                         R (&W)[LA + LB + 1][LA + LB + 1][LA + LB + 1][ncart(LC) * ncart(LD)]) {
+    constexpr int NC = ncart(LC), ND = ncart(LD);
+    constexpr int LAB = LA + LB, LCD = LC + LD, L = LAB + LCD;
+    constexpr int EK = herm_size(LC, LD);
+    constexpr bool KET_S = (LCD == 0);
+    const sq_slots &sl = args.slots;
+    const R *hk = slot_herm_ptr<R>(sl) + kd.hbase;
+    const int pk = kd.pbase, sk = kd.pstride;
+    for (int k = k0; k < k1; ++k) {
+        const PrimPair<R> kt = load_prim<R>(sl, pk + (long long)k * sk);
+        const R q = kt.p;
+        const R X = Px - kt.x;
+        const R Y = Py - kt.y;
+        const R Z = Pz - kt.z;
+        const R Uk = kt.u;
+        const R r = rsqrt_r(p + q);
+        const R alpha = p * q * (r * r);
+        const R T = alpha * (X * X + Y * Y + Z * Z);
+        R F[L + 1];
+        if constexpr (std::is_same<R, double>::value) {
+            boys64<L>(T, args.tab64, F);
+        } else if constexpr (BOYS == BOYS_FP64) {
+            boys_mixed<L>(T, tb0, tb1, F);
+        } else {
+            boys32<L>(T, tb0, tb1, F);
+        }
+        R fac = Uk * r;
+        if constexpr (L == 0) {
+            W[0][0][0][0] = fma(F[0], fac, W[0][0][0][0]);
+        } else {
+            R Fs[L + 1];
+            const R m2a = R(-2) * alpha;
+#pragma unroll
+            for (int n = 0; n <= L; ++n) {
+                Fs[n] = F[n] * fac;
+                if (n < L) fac *= m2a;
+            }
+            R Rt[L + 1][L + 1][L + 1];
+            hermite_r<L, R>(Fs, X, Y, Z, Rt);
+            if constexpr (KET_S) {
+#pragma unroll
+                for (int t = 0; t <= LAB; ++t)
+#pragma unroll
+                    for (int u = 0; u <= LAB - t; ++u)
+#pragma unroll
+                        for (int v = 0; v <= LAB - t - u; ++v) W[t][u][v][0] += Rt[t][u][v];
+            } else {
+                const R *ek = hk + (long long)k * EK * sk;
+#pragma unroll
+                for (int c = 0; c < NC; ++c)
+#pragma unroll
+                    for (int d = 0; d < ND; ++d) {
+                        const int cx = cart_x(LC, c) + cart_x(LD, d);
+                        const int cy = cart_y(LC, c) + cart_y(LD, d);
+                        const int cz = cart_z(LC, c) + cart_z(LD, d);
+                        const int off = herm_offset(LC, LD, c, d);
+#pragma unroll
+                        for (int tau = 0; tau <= cx; ++tau)
+#pragma unroll
+                            for (int nu = 0; nu <= cy; ++nu)
+#pragma unroll
+                                for (int phi = 0; phi <= cz; ++phi) {
+                                    R e = gload(ek + (long long)(off + (tau * (cy + 1) + nu) * (cz + 1) + phi) * sk);
+                                    if ((tau + nu + phi) & 1) e = -e;
+#pragma unroll
+                                    for (int t = 0; t <= LAB; ++t)
+#pragma unroll
+                                        for (int u = 0; u <= LAB - t; ++u)
+#pragma unroll
+                                            for (int v = 0; v <= LAB - t - u; ++v)
+                                                W[t][u][v][c * ND + d] =
+                                                    fma(e, Rt[t + tau][u + nu][v + phi], W[t][u][v][c * ND + d]);
+                                }
+                    }
+            }
+        }
+    }
+}
+
+template <int LA, int LB, int LC, int LD, typename R>
+__device__ __forceinline__ void zero_w(R (&W)[LA + LB + 1][LA + LB + 1][LA + LB + 1][ncart(LC) * ncart(LD)]) {
+    constexpr int LAB = LA + LB, NCD = ncart(LC) * ncart(LD);
+#pragma unroll
+    for (int t = 0; t <= LAB; ++t)
+#pragma unroll
+        for (int u = 0; u <= LAB - t; ++u)
+#pragma unroll
+            for (int v = 0; v <= LAB - t - u; ++v)
+#pragma unroll
+                for (int y = 0; y < NCD; ++y) W[t][u][v][y] = R(0);
+}
+
+// acc[ab][cd] += sum_tuv ub E^{ab}_{tuv}(i) W[tuv][cd] for bra primitive pair
+// i (Hermite values at eb, stride sb), with the bra factor ub = 2 pi^{5/2} U_i.
+template <int LA, int LB, int LC, int LD, typename R>
+__device__ __forceinline__ void bra_transform(const R *eb, int sb, R ub,
+                                              const R (&W)[LA + LB + 1][LA + LB + 1][LA + LB + 1][ncart(LC) * ncart(LD)],
+                                              R (&acc)[ncart(LA) * ncart(LB)][ncart(LC) * ncart(LD)]) {
+    constexpr int NA = ncart(LA), NB = ncart(LB), NCD = ncart(LC) * ncart(LD);
+    if constexpr (LA + LB == 0) {
+#pragma unroll
+        for (int y = 0; y < NCD; ++y) acc[0][y] = fma(ub, W[0][0][0][y], acc[0][y]);
+    } else {
+#pragma unroll
+        for (int a = 0; a < NA; ++a)
+#pragma unroll
+            for (int b = 0; b < NB; ++b) {
+                const int ax = cart_x(LA, a) + cart_x(LB, b);
+                const int ay = cart_y(LA, a) + cart_y(LB, b);
+                const int az = cart_z(LA, a) + cart_z(LB, b);
+                const int off = herm_offset(LA, LB, a, b);
+#pragma unroll
+                for (int t = 0; t <= ax; ++t)
+#pragma unroll
+                    for (int u = 0; u <= ay; ++u)
+#pragma unroll
+                        for (int v = 0; v <= az; ++v) {
+                            const R e = ub * gload(eb + (long long)(off + (t * (ay + 1) + u) * (az + 1) + v) * sb);
+#pragma unroll
+                            for (int y = 0; y < NCD; ++y)
+                                acc[a * NB + b][y] = fma(e, W[t][u][v][y], acc[a * NB + b][y]);
+                        }
+            }
+    }
+}
+
+// The same contraction of an FP32 W, each block element computed in FP32 and
+// then added into the FP64 accumulator.
+template <int LA, int LB, int LC, int LD>
+__device__ __forceinline__ void bra_transform_f32_into_f64(
+    const float *eb, int sb, float ub, const float (&W)[LA + LB + 1][LA + LB + 1][LA + LB + 1][ncart(LC) * ncart(LD)],
+    double (&acc)[ncart(LA) * ncart(LB)][ncart(LC) * ncart(LD)]) {
+    constexpr int NA = ncart(LA), NB = ncart(LB), NCD = ncart(LC) * ncart(LD);
+    if constexpr (LA + LB == 0) {
+#pragma unroll
+        for (int y = 0; y < NCD; ++y) acc[0][y] += f2d_bits(ub * W[0][0][0][y]);
+    } else {
+#pragma unroll
+        for (int a = 0; a < NA; ++a)
+#pragma unroll
+            for (int b = 0; b < NB; ++b) {
+                const int ax = cart_x(LA, a) + cart_x(LB, b);
+                const int ay = cart_y(LA, a) + cart_y(LB, b);
+                const int az = cart_z(LA, a) + cart_z(LB, b);
+                const int off = herm_offset(LA, LB, a, b);
+                float part[NCD];
+#pragma unroll
+                for (int y = 0; y < NCD; ++y) part[y] = 0.0f;
+#pragma unroll
+                for (int t = 0; t <= ax; ++t)
+#pragma unroll
+                    for (int u = 0; u <= ay; ++u)
+#pragma unroll
+                        for (int v = 0; v <= az; ++v) {
+                            const float e = ub * gload(eb + (long long)(off + (t * (ay + 1) + u) * (az + 1) + v) * sb);
+#pragma unroll
+                            for (int y = 0; y < NCD; ++y) part[y] = fmaf(e, W[t][u][v][y], part[y]);
+                        }
+#pragma unroll
+                for (int y = 0; y < NCD; ++y) acc[a * NB + b][y] += f2d_bits(part[y]);
+            }
+    }
+}
+
 // Contracted block of one quartet: acc[a*NB+b][c*ND+d].
 //
 // FP64 work per primitive quartet is what bounds these kernels on GB300, so:
 // the bra factor 2 pi^{5/2} U_bra is applied once per bra primitive pair (in
 // the bra transform), the Hermite coefficients of s-s pairs (exactly 1) are
 // neither loaded nor multiplied, and (ss|ss) accumulates with a single FMA.
-template <int LA, int LB, int LC, int LD, typename R, int BOYS>
-__device__ __forceinline__ void quartet_block(const EriArgs &args, int P, int Q, const float4 *tb0,
-                                              const float4 *tb1,
+//
+// SPLIT (FP64 launches only): primitive-level precision.  Both slots keep
+// their primitive pairs in descending primitive Schwarz factor q, so for bra
+// primitive i the ket primitives with q_i q_k >= tau are a prefix [0, K_i),
+// and K_i does not grow with i.  The prefix runs in FP64; the rest, whose
+// primitive quartets are bounded by tau, runs in FP32 (FP64 Boys recursion,
+// as in SQ_FP32 launches) and its FP32 block is added into the FP64 one.
+template <int LA, int LB, int LC, int LD, typename R, int BOYS, bool SPLIT>
+__device__ __forceinline__ void quartet_block(const EriArgs &args, const SlotDesc &bd, const SlotDesc &kd,
+                                              const float4 *tb0, const float4 *tb1,
                                               R (&acc)[ncart(LA) * ncart(LB)][ncart(LC) * ncart(LD)]) {
-    constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
-    constexpr int NAB = NA * NB, NCD = NC * ND;
-    constexpr int LAB = LA + LB, LCD = LC + LD, L = LAB + LCD;
-    constexpr int EB = herm_size(LA, LB), EK = herm_size(LC, LD);
-    constexpr bool BRA_S = (LAB == 0), KET_S = (LCD == 0);
-
-    // slot layout: field f of primitive pair i of slot s at prim[f*NPP + pbase[s] + i*pstride[s]]
+    static_assert(!SPLIT || std::is_same<R, double>::value, "primitive-level precision splits FP64 launches");
+    constexpr int NAB = ncart(LA) * ncart(LB), NCD = ncart(LC) * ncart(LD);
+    constexpr int LAB = LA + LB;
+    constexpr int EB = herm_size(LA, LB);
     const sq_slots &sl = args.slots;
-    const R *prim = slot_prim_ptr<R>(sl);
-    const R *herm = slot_herm_ptr<R>(sl);
-    const long long NPP = sl.npp_total;
-    const int nb = gload(sl.npp + P), nk = gload(sl.npp + Q);
-    const int pb = gload(sl.pbase + P), sb = gload(sl.pstride + P);
-    const int pk = gload(sl.pbase + Q), sk = gload(sl.pstride + Q);
-    const R *hb = herm + gload(sl.hbase + P);
-    const R *hk = herm + gload(sl.hbase + Q);
+    const int nb = bd.npp, nk = kd.npp;
+    const int pb = bd.pbase, sb = bd.pstride;
+    const R *hb = slot_herm_ptr<R>(sl) + bd.hbase;
 
 #pragma unroll
     for (int x = 0; x < NAB; ++x)
 #pragma unroll
         for (int y = 0; y < NCD; ++y) acc[x][y] = R(0);
 
+    int K = nk;  // FP64 ket prefix of the current bra primitive (SPLIT)
     for (int i = 0; i < nb; ++i) {
         const long long ib = pb + (long long)i * sb;
-        const R p = gload(prim + ib);
-        const R Px = gload(prim + NPP + ib), Py = gload(prim + 2 * NPP + ib), Pz = gload(prim + 3 * NPP + ib);
-        const R Ub = gload(prim + 4 * NPP + ib);
-        R W[LAB + 1][LAB + 1][LAB + 1][NCD];
-#pragma unroll
-        for (int t = 0; t <= LAB; ++t)
-#pragma unroll
-            for (int u = 0; u <= LAB - t; ++u)
-#pragma unroll
-                for (int v = 0; v <= LAB - t - u; ++v)
-#pragma unroll
-                    for (int y = 0; y < NCD; ++y) W[t][u][v][y] = R(0);
-
-        for (int k = 0; k < nk; ++k) {
-            const long long ik = pk + (long long)k * sk;
-            const R q = gload(prim + ik);
-            const R X = Px - gload(prim + NPP + ik);
-            const R Y = Py - gload(prim + 2 * NPP + ik);
-            const R Z = Pz - gload(prim + 3 * NPP + ik);
-            const R Uk = gload(prim + 4 * NPP + ik);
-            const R r = rsqrt_r(p + q);
-            const R alpha = p * q * (r * r);
-            const R T = alpha * (X * X + Y * Y + Z * Z);
-            R F[L + 1];
-            if constexpr (std::is_same<R, double>::value) {
-                boys64<L>(T, args.tab64, F);
-            } else if constexpr (BOYS == BOYS_FP64) {
-                boys_mixed<L>(T, tb0, tb1, F);
-            } else {
-                boys32<L>(T, tb0, tb1, F);
-            }
-            R fac = Uk * r;
-            if constexpr (L == 0) {
-                W[0][0][0][0] = fma(F[0], fac, W[0][0][0][0]);
-            } else {
-                R Fs[L + 1];
-                const R m2a = R(-2) * alpha;
-#pragma unroll
-                for (int n = 0; n <= L; ++n) {
-                    Fs[n] = F[n] * fac;
-                    if (n < L) fac *= m2a;
-                }
-                R Rt[L + 1][L + 1][L + 1];
-                hermite_r<L, R>(Fs, X, Y, Z, Rt);
-                if constexpr (KET_S) {
-#pragma unroll
-                    for (int t = 0; t <= LAB; ++t)
-#pragma unroll
-                        for (int u = 0; u <= LAB - t; ++u)
-#pragma unroll
-                            for (int v = 0; v <= LAB - t - u; ++v) W[t][u][v][0] += Rt[t][u][v];
-                } else {
-                    // W[tuv][cd] += sum_{tau nu phi} (-1)^{tau+nu+phi} E^{cd}_{tau nu phi} R[t+tau][u+nu][v+phi]
-                    const R *ek = hk + (long long)k * EK * sk;
-#pragma unroll
-                    for (int c = 0; c < NC; ++c)
-#pragma unroll
-                        for (int d = 0; d < ND; ++d) {
-                            const int cx = cart_x(LC, c) + cart_x(LD, d);
-                            const int cy = cart_y(LC, c) + cart_y(LD, d);
-                            const int cz = cart_z(LC, c) + cart_z(LD, d);
-                            const int off = herm_offset(LC, LD, c, d);
-#pragma unroll
-                            for (int tau = 0; tau <= cx; ++tau)
-#pragma unroll
-                                for (int nu = 0; nu <= cy; ++nu)
-#pragma unroll
-                                    for (int phi = 0; phi <= cz; ++phi) {
-                                        R e = gload(ek + (long long)(off + (tau * (cy + 1) + nu) * (cz + 1) + phi) * sk);
-                                        if ((tau + nu + phi) & 1) e = -e;
-#pragma unroll
-                                        for (int t = 0; t <= LAB; ++t)
-#pragma unroll
-                                            for (int u = 0; u <= LAB - t; ++u)
-#pragma unroll
-                                                for (int v = 0; v <= LAB - t - u; ++v)
-                                                    W[t][u][v][c * ND + d] =
-                                                        fma(e, Rt[t + tau][u + nu][v + phi], W[t][u][v][c * ND + d]);
-                                    }
-                        }
-                }
-            }
+        const PrimPair<R> br = load_prim<R>(sl, ib);
+        if constexpr (SPLIT) {
+            const float thr = args.prim_tau / __ldg(sl.prim32v + 8 * ib + 5);
+            while (K > 0 && __ldg(sl.prim32v + 8 * (kd.pbase + (long long)(K - 1) * kd.pstride) + 5) < thr) --K;
         }
-        // bra transform with the bra factor 2 pi^{5/2} U_bra
-        const R ub = R(kTwoPi52) * Ub;
-        if constexpr (BRA_S) {
-#pragma unroll
-            for (int y = 0; y < NCD; ++y) acc[0][y] = fma(ub, W[0][0][0][y], acc[0][y]);
-        } else {
-            const R *eb = hb + (long long)i * EB * sb;
-#pragma unroll
-            for (int a = 0; a < NA; ++a)
-#pragma unroll
-                for (int b = 0; b < NB; ++b) {
-                    const int ax = cart_x(LA, a) + cart_x(LB, b);
-                    const int ay = cart_y(LA, a) + cart_y(LB, b);
-                    const int az = cart_z(LA, a) + cart_z(LB, b);
-                    const int off = herm_offset(LA, LB, a, b);
-#pragma unroll
-                    for (int t = 0; t <= ax; ++t)
-#pragma unroll
-                        for (int u = 0; u <= ay; ++u)
-#pragma unroll
-                            for (int v = 0; v <= az; ++v) {
-                                const R e = ub * gload(eb + (long long)(off + (t * (ay + 1) + u) * (az + 1) + v) * sb);
-#pragma unroll
-                                for (int y = 0; y < NCD; ++y)
-                                    acc[a * NB + b][y] = fma(e, W[t][u][v][y], acc[a * NB + b][y]);
-                            }
-                }
+        if (!SPLIT || K > 0) {
+            R W[LAB + 1][LAB + 1][LAB + 1][NCD];
+            zero_w<LA, LB, LC, LD, R>(W);
+            ket_loop<LA, LB, LC, LD, R, BOYS>(args, br.p, br.x, br.y, br.z, kd, 0, SPLIT ? K : nk, tb0, tb1, W);
+            bra_transform<LA, LB, LC, LD, R>(hb + (long long)i * EB * sb, sb, R(kTwoPi52) * br.u, W, acc);
+        }
+        if constexpr (SPLIT) {
+            if (K < nk) {
+                const float4 b4 = __ldg(reinterpret_cast<const float4 *>(sl.prim32v) + 2 * ib);
+                const float ub = (float)kTwoPi52 * __ldg(sl.prim32v + 8 * ib + 4);
+                float W32[LAB + 1][LAB + 1][LAB + 1][NCD];
+                zero_w<LA, LB, LC, LD, float>(W32);
+                ket_loop<LA, LB, LC, LD, float, BOYS_FP64>(args, b4.x, b4.y, b4.z, b4.w, kd, K, nk, tb0, tb1, W32);
+                bra_transform_f32_into_f64<LA, LB, LC, LD>(sl.herm32 + bd.hbase + (long long)i * EB * sb, sb, ub,
+                                                           W32, acc);
+            }
         }
     }
 }
 
-template <int LA, int LB, int LC, int LD, typename R, int BOYS, int MODE>
-__global__ void __launch_bounds__(128) eri_class_kernel(const EriArgs args) {
+// The six density blocks of one quartet (rows/columns of shells a, b, c, d).
+template <int NA, int NB, int NC, int ND, typename R>
+struct DensityBlocks {
+    R ab[NA][NB], cd[NC][ND], ac[NA][NC], ad[NA][ND], bc[NB][NC], bd[NB][ND];
+};
+
+// Matrix element index of (row ra + i, column oc + j): ra = mb + oa*ld is
+// the first row's offset of shell a in the molecule's block.  32-bit: the
+// J/K entry points refuse matrices of 2^31 elements or more.
+struct QuartetRows {
+    int ra, rb, rc;      // row offsets of shells a, b, c
+    int oa, ob, oc, od;  // first column of each shell
+    int ld;
+};
+
+__device__ __forceinline__ QuartetRows quartet_rows(const sq_slots &sl, int P, const SlotDesc &bd, const SlotDesc &kd) {
+    const int mb = sl.mbase ? (int)__ldg(sl.mbase + P) : 0;
+    QuartetRows w;
+    w.ld = bd.ld;
+    w.oa = bd.oa;
+    w.ob = bd.ob;
+    w.oc = kd.oa;
+    w.od = kd.ob;
+    w.ra = mb + bd.oa * w.ld;
+    w.rb = mb + bd.ob * w.ld;
+    w.rc = mb + kd.oa * w.ld;
+    return w;
+}
+
+template <int NA, int NB, int NC, int ND, typename R>
+__device__ __forceinline__ void load_density(const R *D, const QuartetRows &w, DensityBlocks<NA, NB, NC, ND, R> &x) {
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+        for (int b = 0; b < NB; ++b) x.ab[a][b] = gload(D + w.ra + a * w.ld + w.ob + b);
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+        for (int d = 0; d < ND; ++d) x.cd[c][d] = gload(D + w.rc + c * w.ld + w.od + d);
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+        for (int c = 0; c < NC; ++c) x.ac[a][c] = gload(D + w.ra + a * w.ld + w.oc + c);
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+        for (int d = 0; d < ND; ++d) x.ad[a][d] = gload(D + w.ra + a * w.ld + w.od + d);
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int c = 0; c < NC; ++c) x.bc[b][c] = gload(D + w.rb + b * w.ld + w.oc + c);
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int d = 0; d < ND; ++d) x.bd[b][d] = gload(D + w.rb + b * w.ld + w.od + d);
+}
+
+// Digest one contracted block into Jacc/Kacc (one density):
+//   Jacc[ab] += wJ sum_cd v D[cd],  Jacc[cd] += wJ sum_ab v D[ab],
+//   Kacc[ac] += wK sum_bd v D[bd],  Kacc[bd] += wK v D[ac],  Kacc[ad] += wK v D[bc],  Kacc[bc] += wK v D[ad].
+template <int NA, int NB, int NC, int ND, typename R>
+__device__ __forceinline__ void digest_blocks(const R (&acc)[NA * NB][NC * ND], const R (&Dab)[NA][NB],
+                                              const R (&Dcd)[NC][ND], const R (&Dac)[NA][NC], const R (&Dad)[NA][ND],
+                                              const R (&Dbc)[NB][NC], const R (&Dbd)[NB][ND], const QuartetRows &w, R wJ,
+                                              R wK, double *J, double *K) {
+    R Jab[NA][NB], Jcd[NC][ND], Kac[NA][NC], Kad[NA][ND], Kbc[NB][NC], Kbd[NB][ND];
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+        for (int b = 0; b < NB; ++b) Jab[a][b] = R(0);
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+        for (int d = 0; d < ND; ++d) Jcd[c][d] = R(0);
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+        for (int c = 0; c < NC; ++c) Kac[a][c] = R(0);
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+        for (int d = 0; d < ND; ++d) Kad[a][d] = R(0);
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int c = 0; c < NC; ++c) Kbc[b][c] = R(0);
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int d = 0; d < ND; ++d) Kbd[b][d] = R(0);
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+        for (int b = 0; b < NB; ++b)
+#pragma unroll
+            for (int c = 0; c < NC; ++c)
+#pragma unroll
+                for (int d = 0; d < ND; ++d) {
+                    const R v = acc[a * NB + b][c * ND + d];
+                    Jab[a][b] = fma(v, Dcd[c][d], Jab[a][b]);
+                    Jcd[c][d] = fma(v, Dab[a][b], Jcd[c][d]);
+                    Kac[a][c] = fma(v, Dbd[b][d], Kac[a][c]);
+                    Kbd[b][d] = fma(v, Dac[a][c], Kbd[b][d]);
+                    Kad[a][d] = fma(v, Dbc[b][c], Kad[a][d]);
+                    Kbc[b][c] = fma(v, Dad[a][d], Kbc[b][c]);
+                }
+    auto to_d = [](R x) -> double {
+        if constexpr (std::is_same<R, double>::value)
+            return x;
+        else
+            return f2d_bits(x);
+    };
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+        for (int b = 0; b < NB; ++b) atomicAdd(J + w.ra + a * w.ld + w.ob + b, to_d(wJ * Jab[a][b]));
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+        for (int d = 0; d < ND; ++d) atomicAdd(J + w.rc + c * w.ld + w.od + d, to_d(wJ * Jcd[c][d]));
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+        for (int c = 0; c < NC; ++c) atomicAdd(K + w.ra + a * w.ld + w.oc + c, to_d(wK * Kac[a][c]));
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int d = 0; d < ND; ++d) atomicAdd(K + w.rb + b * w.ld + w.od + d, to_d(wK * Kbd[b][d]));
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+        for (int d = 0; d < ND; ++d) atomicAdd(K + w.ra + a * w.ld + w.od + d, to_d(wK * Kad[a][d]));
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int c = 0; c < NC; ++c) atomicAdd(K + w.rb + b * w.ld + w.oc + c, to_d(wK * Kbc[b][c]));
+}
+
+// Light classes: density blocks loaded before the primitive loops.
+template <int NA, int NB, int NC, int ND, typename R>
+__device__ __forceinline__ void digest(const R (&acc)[NA * NB][NC * ND], const DensityBlocks<NA, NB, NC, ND, R> &Dx,
+                                       const QuartetRows &w, R wJ, R wK, double *J, double *K) {
+    digest_blocks<NA, NB, NC, ND, R>(acc, Dx.ab, Dx.cd, Dx.ac, Dx.ad, Dx.bc, Dx.bd, w, wJ, wK, J, K);
+}
+
+// Heavy classes: density blocks loaded after the primitive loops.
+template <int NA, int NB, int NC, int ND, typename R>
+__device__ __forceinline__ void digest_loading(const R (&acc)[NA * NB][NC * ND], const R *D, const QuartetRows &w,
+                                               R wJ, R wK, double *J, double *K) {
+    DensityBlocks<NA, NB, NC, ND, R> Dx;
+    load_density(D, w, Dx);
+    digest<NA, NB, NC, ND, R>(acc, Dx, w, wJ, wK, J, K);
+}
+
+// Minimum resident blocks asked of ptxas: none for the light classes (their
+// own register count, which keeps occupancy), one for L >= 5, whose blocks
+// spill anyway: without it ptxas allocated only 32 registers to the FP64
+// (dd|ds) kernel and spilled four times as much.
+__host__ __device__ constexpr int kMinBlocks(int L) { return L >= 5 ? 1 : 0; }
+
+// Per-thread J/K kernel: one contracted quartet (or sub-slot chunk) per
+// thread, grid-stride over the class's quartet list.  Each quartet starts
+// from its two slot descriptors.  For the light classes the whole
+// descriptors and the six density blocks are loaded before the primitive
+// loops, so that their latency hides behind the integral arithmetic; the
+// heavy classes load the epilogue fields only after the loops.
+template <int LA, int LB, int LC, int LD, typename R, int BOYS, int MODE, bool SPLIT = false>
+__global__ void __launch_bounds__(128, kMinBlocks(LA + LB + LC + LD)) eri_class_kernel(const EriArgs args) {
+    static_assert(MODE == MODE_JK, "per-thread kernels serve J/K launches only");
     constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
     constexpr int NAB = NA * NB, NCD = NC * ND;
     constexpr int L = LA + LB + LC + LD;
-    // FP32 launches read the two Boys Taylor blocks they need from shared memory
-    // (random rows: one smem wavefront per 8 lanes instead of one L1 sector per lane).
-    __shared__ float4 s_tab[std::is_same<R, float>::value ? 2 : 1][std::is_same<R, float>::value ? SQ_BOYS_NGRID : 1];
+    constexpr int NDENS = NAB + NCD + NA * NC + NA * ND + NB * NC + NB * ND;
+    constexpr bool PREFETCH_D = NDENS <= 32;
+    // FP32 launches (and the FP32 part of split FP64 launches) read the two
+    // Boys Taylor blocks they need from shared memory (random rows: one smem
+    // wavefront per 8 lanes instead of one L1 sector per lane).
+    constexpr bool TAB32 = std::is_same<R, float>::value || SPLIT;
+    __shared__ float4 s_tab[TAB32 ? 2 : 1][TAB32 ? SQ_BOYS_NGRID : 1];
     const float4 *tb0 = nullptr, *tb1 = nullptr;
-    if constexpr (std::is_same<R, float>::value) {
+    if constexpr (TAB32) {
         const float4 *g = reinterpret_cast<const float4 *>(args.tab32 + SQ_BOYS_TAY32_OFF);
         const int blk0 = boys32_block<L>(0), blk1 = boys32_block<L>(1);
         for (int x = threadIdx.x; x < SQ_BOYS_NGRID; x += blockDim.x) {
@@ -310,163 +614,46 @@ __global__ void __launch_bounds__(128) eri_class_kernel(const EriArgs args) {
         tb0 = s_tab[0];
         tb1 = s_tab[1];
     }
+    const int nd = args.nd > 1 ? args.nd : 1;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long qi = (long long)blockIdx.x * blockDim.x + threadIdx.x; qi < args.nq; qi += stride) {
         const int2 pq = args.quartets[qi];
-        const int P = pq.x, Q = pq.y;
+        SlotDesc bd = PREFETCH_D ? load_desc(args.slots.desc, pq.x) : load_desc_prims(args.slots.desc, pq.x);
+        SlotDesc kd = PREFETCH_D ? load_desc(args.slots.desc, pq.y) : load_desc_prims(args.slots.desc, pq.y);
+        const R *D0;
+        if constexpr (std::is_same<R, double>::value)
+            D0 = args.D;
+        else
+            D0 = args.D32;
+        QuartetRows w;
+        DensityBlocks<NA, NB, PREFETCH_D ? NC : 1, PREFETCH_D ? ND : 1, R> Dx;
+        if constexpr (PREFETCH_D) {
+            w = quartet_rows(args.slots, pq.x, bd, kd);
+            load_density(D0, w, Dx);
+        }
+
         R acc[NAB][NCD];
-        quartet_block<LA, LB, LC, LD, R, BOYS>(args, P, Q, tb0, tb1, acc);
+        quartet_block<LA, LB, LC, LD, R, BOYS, SPLIT>(args, bd, kd, tb0, tb1, acc);
+        if constexpr (!PREFETCH_D) {
+            load_desc_epilogue(args.slots.desc, pq.x, bd);
+            load_desc_epilogue(args.slots.desc, pq.y, kd);
+            w = quartet_rows(args.slots, pq.x, bd, kd);
+        }
 
-        const int pairP = gload(args.slots.pair + P), pairQ = gload(args.slots.pair + Q);
-        const int sa = gload(args.pairs.shells + 2 * pairP), sb = gload(args.pairs.shells + 2 * pairP + 1);
-        const int sc = gload(args.pairs.shells + 2 * pairQ), sd = gload(args.pairs.shells + 2 * pairQ + 1);
-        const int oa = gload(args.basis.bf_off + sa), ob = gload(args.basis.bf_off + sb);
-        const int oc = gload(args.basis.bf_off + sc), od = gload(args.basis.bf_off + sd);
-        const long long n = args.basis.nbf;
-
-        if constexpr (MODE == MODE_SCHWARZ) {
-            R mx = acc[0][0];
-#pragma unroll
-            for (int x = 0; x < NAB; ++x)
-#pragma unroll
-                for (int y = 0; y < NCD; ++y) mx = acc[x][y] > mx ? acc[x][y] : mx;
-            args.q[P] = sqrt((double)mx);
-        } else if constexpr (MODE == MODE_DENSE) {
-            double *V = args.V;
-#pragma unroll
-            for (int a = 0; a < NA; ++a)
-#pragma unroll
-                for (int b = 0; b < NB; ++b)
-#pragma unroll
-                    for (int c = 0; c < NC; ++c)
-#pragma unroll
-                        for (int d = 0; d < ND; ++d) {
-                            const double v = acc[a * NB + b][c * ND + d];
-                            const long long A = oa + a, B = ob + b, C = oc + c, Dd = od + d;
-                            V[((A * n + B) * n + C) * n + Dd] = v;
-                            V[((B * n + A) * n + C) * n + Dd] = v;
-                            V[((A * n + B) * n + Dd) * n + C] = v;
-                            V[((B * n + A) * n + Dd) * n + C] = v;
-                            V[((C * n + Dd) * n + A) * n + B] = v;
-                            V[((Dd * n + C) * n + A) * n + B] = v;
-                            V[((C * n + Dd) * n + B) * n + A] = v;
-                            V[((Dd * n + C) * n + B) * n + A] = v;
-                        }
-        } else {
-            // Permutational weight m = 8 / 2^{[a==b] + [c==d] + [P==Q]}; J gets m/2, K gets m/4.
-            double m = 8.0;
-            if (sa == sb) m *= 0.5;
-            if (sc == sd) m *= 0.5;
-            if (pairP == pairQ) m *= 0.5;  // sub-slots of a pair count as that pair
-            const R wJ = R(0.5 * m), wK = R(0.25 * m);
-            const int nd = args.nd > 1 ? args.nd : 1;
-            for (int di = 0; di < nd; ++di) {
-            const R *D;
-            if constexpr (std::is_same<R, double>::value)
-                D = args.D + di * args.dstride;
-            else
-                D = args.D32 + di * args.dstride;
-            R Dab[NA][NB], Dcd[NC][ND], Dac[NA][NC], Dad[NA][ND], Dbc[NB][NC], Dbd[NB][ND];
-            const sq_basis &bs = args.basis;
-#pragma unroll
-            for (int a = 0; a < NA; ++a)
-#pragma unroll
-                for (int b = 0; b < NB; ++b) Dab[a][b] = gload(D + mat_index(bs, sa, a, sb, b));
-#pragma unroll
-            for (int c = 0; c < NC; ++c)
-#pragma unroll
-                for (int d = 0; d < ND; ++d) Dcd[c][d] = gload(D + mat_index(bs, sc, c, sd, d));
-#pragma unroll
-            for (int a = 0; a < NA; ++a)
-#pragma unroll
-                for (int c = 0; c < NC; ++c) Dac[a][c] = gload(D + mat_index(bs, sa, a, sc, c));
-#pragma unroll
-            for (int a = 0; a < NA; ++a)
-#pragma unroll
-                for (int d = 0; d < ND; ++d) Dad[a][d] = gload(D + mat_index(bs, sa, a, sd, d));
-#pragma unroll
-            for (int b = 0; b < NB; ++b)
-#pragma unroll
-                for (int c = 0; c < NC; ++c) Dbc[b][c] = gload(D + mat_index(bs, sb, b, sc, c));
-#pragma unroll
-            for (int b = 0; b < NB; ++b)
-#pragma unroll
-                for (int d = 0; d < ND; ++d) Dbd[b][d] = gload(D + mat_index(bs, sb, b, sd, d));
-
-            R Jab[NA][NB], Jcd[NC][ND], Kac[NA][NC], Kad[NA][ND], Kbc[NB][NC], Kbd[NB][ND];
-#pragma unroll
-            for (int a = 0; a < NA; ++a)
-#pragma unroll
-                for (int b = 0; b < NB; ++b) Jab[a][b] = R(0);
-#pragma unroll
-            for (int c = 0; c < NC; ++c)
-#pragma unroll
-                for (int d = 0; d < ND; ++d) Jcd[c][d] = R(0);
-#pragma unroll
-            for (int a = 0; a < NA; ++a)
-#pragma unroll
-                for (int c = 0; c < NC; ++c) Kac[a][c] = R(0);
-#pragma unroll
-            for (int a = 0; a < NA; ++a)
-#pragma unroll
-                for (int d = 0; d < ND; ++d) Kad[a][d] = R(0);
-#pragma unroll
-            for (int b = 0; b < NB; ++b)
-#pragma unroll
-                for (int c = 0; c < NC; ++c) Kbc[b][c] = R(0);
-#pragma unroll
-            for (int b = 0; b < NB; ++b)
-#pragma unroll
-                for (int d = 0; d < ND; ++d) Kbd[b][d] = R(0);
-
-#pragma unroll
-            for (int a = 0; a < NA; ++a)
-#pragma unroll
-                for (int b = 0; b < NB; ++b)
-#pragma unroll
-                    for (int c = 0; c < NC; ++c)
-#pragma unroll
-                        for (int d = 0; d < ND; ++d) {
-                            const R v = acc[a * NB + b][c * ND + d];
-                            Jab[a][b] = fma(v, Dcd[c][d], Jab[a][b]);
-                            Jcd[c][d] = fma(v, Dab[a][b], Jcd[c][d]);
-                            Kac[a][c] = fma(v, Dbd[b][d], Kac[a][c]);
-                            Kbd[b][d] = fma(v, Dac[a][c], Kbd[b][d]);
-                            Kad[a][d] = fma(v, Dbc[b][c], Kad[a][d]);
-                            Kbc[b][c] = fma(v, Dad[a][d], Kbc[b][c]);
-                        }
-            double *J = args.Jacc + di * args.dstride, *K = args.Kacc + di * args.dstride;
-            auto to_d = [](R x) -> double {
-                if constexpr (std::is_same<R, double>::value)
-                    return x;
-                else
-                    return f2d_bits(x);
-            };
-#pragma unroll
-            for (int a = 0; a < NA; ++a)
-#pragma unroll
-                for (int b = 0; b < NB; ++b) atomicAdd(J + mat_index(bs, sa, a, sb, b), to_d(wJ * Jab[a][b]));
-#pragma unroll
-            for (int c = 0; c < NC; ++c)
-#pragma unroll
-                for (int d = 0; d < ND; ++d) atomicAdd(J + mat_index(bs, sc, c, sd, d), to_d(wJ * Jcd[c][d]));
-#pragma unroll
-            for (int a = 0; a < NA; ++a)
-#pragma unroll
-                for (int c = 0; c < NC; ++c) atomicAdd(K + mat_index(bs, sa, a, sc, c), to_d(wK * Kac[a][c]));
-#pragma unroll
-            for (int b = 0; b < NB; ++b)
-#pragma unroll
-                for (int d = 0; d < ND; ++d) atomicAdd(K + mat_index(bs, sb, b, sd, d), to_d(wK * Kbd[b][d]));
-#pragma unroll
-            for (int a = 0; a < NA; ++a)
-#pragma unroll
-                for (int d = 0; d < ND; ++d) atomicAdd(K + mat_index(bs, sa, a, sd, d), to_d(wK * Kad[a][d]));
-#pragma unroll
-            for (int b = 0; b < NB; ++b)
-#pragma unroll
-                for (int c = 0; c < NC; ++c) atomicAdd(K + mat_index(bs, sb, b, sc, c), to_d(wK * Kbc[b][c]));
-            }  // densities
+        // Permutational weight m = 8 / 2^{[a==b] + [c==d] + [P==Q]}; J gets m/2, K gets m/4.
+        double m = 8.0;
+        if ((bd.pairf >> 30) & 1) m *= 0.5;
+        if ((kd.pairf >> 30) & 1) m *= 0.5;
+        if (bd.pairf == kd.pairf) m *= 0.5;  // sub-slots of a pair count as that pair
+        const R wJ = R(0.5 * m), wK = R(0.25 * m);
+        for (int di = 0; di < nd; ++di) {
+            double *Jd = args.Jacc + di * args.dstride, *Kd = args.Kacc + di * args.dstride;
+            if constexpr (PREFETCH_D) {
+                if (di > 0) load_density(D0 + di * args.dstride, w, Dx);
+                digest<NA, NB, NC, ND, R>(acc, Dx, w, wJ, wK, Jd, Kd);
+            } else {
+                digest_loading<NA, NB, NC, ND, R>(acc, D0 + di * args.dstride, w, wJ, wK, Jd, Kd);
+            }
         }
     }
 }
@@ -481,11 +668,14 @@ cudaError_t launch_eri_class(const EriArgs &args, int mode, int precision, cudaS
     long long blocks = (args.nq + threads - 1) / threads;
     // FP64: many blocks (FP64-bound, heavy-first order balances); FP32: about
     // two waves of persistent blocks so the shared Boys table is loaded rarely.
-    const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : (precision == SQ_FP64 ? sm_count() * 16 * 8 : sm_count() * 16);
+    const bool fp64 = precision == SQ_FP64 || precision == SQ_FP64_PRIM;
+    const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : (fp64 ? sm_count() * 16 * 8 : sm_count() * 16);
     if (blocks > cap) blocks = cap;
     (void)mode;  // per-thread kernels serve J/K launches only
     if (precision == SQ_FP64)
         eri_class_kernel<LA, LB, LC, LD, double, BOYS_FP64, MODE_JK><<<(int)blocks, threads, 0, stream>>>(args);
+    else if (precision == SQ_FP64_PRIM)
+        eri_class_kernel<LA, LB, LC, LD, double, BOYS_FP64, MODE_JK, true><<<(int)blocks, threads, 0, stream>>>(args);
     else if (precision == SQ_FP32)
         eri_class_kernel<LA, LB, LC, LD, float, BOYS_FP64, MODE_JK><<<(int)blocks, threads, 0, stream>>>(args);
     else

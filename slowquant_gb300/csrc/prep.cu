@@ -363,6 +363,12 @@ __global__ void slots_fill_kernel(const sq_basis basis, const sq_pairs pairs, sq
             const double v = pairs.prim[8 * (src + kk) + f];
             slots.prim[f * NPP + dst] = v;
             if (slots.prim32) slots.prim32[f * NPP + dst] = (float)v;
+            if (slots.prim32v) slots.prim32v[8 * dst + f] = (float)v;
+        }
+        if (slots.prim32v) {
+            slots.prim32v[8 * dst + 5] = pairs.pq ? (float)pairs.pq[src + kk] : 0.0f;
+            slots.prim32v[8 * dst + 6] = 0.0f;
+            slots.prim32v[8 * dst + 7] = 0.0f;
         }
         for (int e = 0; e < E; ++e) {
             const double v = pairs.herm[hsrc + (long long)kk * E + e];
@@ -371,6 +377,24 @@ __global__ void slots_fill_kernel(const sq_basis basis, const sq_pairs pairs, sq
             if (slots.herm32) slots.herm32[d] = (float)v;
         }
     }
+}
+
+// Slot descriptor (see sq_slots::desc): one thread per slot.
+__global__ void slots_describe_kernel(const sq_basis basis, const sq_pairs pairs, sq_slots slots) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= slots.nslot) return;
+    const int P = slots.pair[s];
+    const int a = pairs.shells[2 * P], b = pairs.shells[2 * P + 1];
+    int *d = slots.desc + 8 * (long long)s;
+    d[0] = slots.npp[s];
+    d[1] = slots.pbase[s];
+    d[2] = slots.pstride[s];
+    d[3] = (int)slots.hbase[s];
+    d[4] = basis.bf_off[a];
+    d[5] = basis.bf_off[b];
+    d[6] = P | (a == b ? (1 << 30) : 0);
+    d[7] = basis.mat_base == nullptr ? basis.nbf : basis.mat_ld[a];
+    if (basis.mat_base != nullptr) slots.mbase[s] = basis.mat_base[a];
 }
 
 __global__ void fock_build_kernel(int nbf, const double *H, const double *Jacc, const double *Kacc, double *F,
@@ -456,6 +480,19 @@ extern "C" int sq_slots_fill(const sq_basis *basis, const sq_pairs *pairs, sq_sl
     if (slots->nslot <= 0) return SQ_OK;
     slots_fill_kernel<<<(slots->nslot + 127) / 128, 128, 0, (cudaStream_t)stream>>>(*basis, *pairs, *slots);
     return check_launch("sq_slots_fill");
+}
+
+extern "C" int sq_slots_describe(const sq_basis *basis, const sq_pairs *pairs, sq_slots *slots, void *stream) {
+    if (!basis || !pairs || !slots || !slots->pair || !slots->npp || !slots->pbase || !slots->pstride ||
+        !slots->hbase || !slots->desc || !pairs->shells ||
+        (basis->mat_base != nullptr && (!basis->mat_ld || !slots->mbase)))
+        return set_error(SQ_ERR_ARG, "sq_slots_describe: bad argument");
+    if (slots->nherm_total >= (1LL << 31) || pairs->npair >= (1 << 30))
+        return set_error(SQ_ERR_ARG, "sq_slots_describe: %lld Hermite values / %d pairs exceed the descriptor's "
+                         "32-bit fields", slots->nherm_total, pairs->npair);
+    if (slots->nslot <= 0) return SQ_OK;
+    slots_describe_kernel<<<(slots->nslot + 127) / 128, 128, 0, (cudaStream_t)stream>>>(*basis, *pairs, *slots);
+    return check_launch("sq_slots_describe");
 }
 
 extern "C" int sq_fock_build(int nbf, const double *H, const double *Jacc, const double *Kacc, double *F, double *J,

@@ -447,6 +447,12 @@ class IntegralEngine:
         self.t_slot_herm = torch.empty(max(hoff, 1), dtype=torch.float64, device=dev)
         self.t_slot_prim32 = torch.empty(max(5 * poff, 1), dtype=torch.float32, device=dev) if self.fp32 else None
         self.t_slot_herm32 = torch.empty(max(hoff, 1), dtype=torch.float32, device=dev) if self.fp32 else None
+        self.t_slot_prim32v = torch.empty(max(8 * poff, 1), dtype=torch.float32, device=dev) if self.fp32 else None
+        self.t_slot_desc = torch.empty(max(8 * nslot, 8), dtype=torch.int32, device=dev)
+        # primitive Schwarz factors in the pair table's order, copied into the packed FP32 slot data
+        self.t_prim_q = torch.tensor(self.prim_q if len(self.prim_q) else np.zeros(1), dtype=torch.float64,
+                                     device=dev)
+        self.cpairs.pq = ptr(self.t_prim_q)
         s = SqSlots()
         s.nslot, s.npp_total, s.nherm_total = nslot, poff, hoff
         s.pair, s.npp, s.pbase, s.pstride, s.hbase = (ptr(self.t_slot_pair), ptr(self.t_slot_npp),
@@ -456,6 +462,7 @@ class IntegralEngine:
         s.prim32, s.herm32 = ptr(self.t_slot_prim32), ptr(self.t_slot_herm32)
         s.prim_src, s.prim_src_off = ptr(self.t_slot_prim_src), ptr(self.t_slot_prim_src_off)
         s.sub = ptr(self.t_slot_sub)
+        s.desc, s.mbase, s.prim32v = ptr(self.t_slot_desc), None, ptr(self.t_slot_prim32v)
         self._slots = s
         if self.nslot_base:
             # fill the parents' data only: sub-slots point into it
@@ -463,6 +470,8 @@ class IntegralEngine:
             fill.nslot = self.nslot_base
             check(self.lib.sq_slots_fill(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(fill),
                                          self._stream()), "sq_slots_fill")
+            check(self.lib.sq_slots_describe(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(s),
+                                             self._stream()), "sq_slots_describe")
 
     # -------------------------------------------------------------- quartets
     def quartets(self, threshold: float, fp32_threshold: float | None = None, q: np.ndarray | None = None,
@@ -699,8 +708,10 @@ class IntegralEngine:
             )
         return self._jk_scratch
 
-    def jk_accumulate(self, D: torch.Tensor, lists, precisions, Jacc=None, Kacc=None):
-        """Run sq_jk for each (quartet list, precision); returns (Jacc, Kacc)."""
+    def jk_accumulate(self, D: torch.Tensor, lists, precisions, Jacc=None, Kacc=None, prim_tau: float = 0.0):
+        """Run sq_jk for each (quartet list, precision); returns (Jacc, Kacc).
+
+        Precision "fp64_prim" runs sq_jk_prim with bound ``prim_tau``."""
         Ja, Ka, D32 = self._scratch()
         if Jacc is None:
             Jacc, Kacc = Ja, Ka
@@ -717,6 +728,11 @@ class IntegralEngine:
         for i, (ql, prec) in enumerate(work):
             s = main if i == 0 else side[i - 1]
             qs = ql.cstruct()
+            if prec == "fp64_prim":
+                check(self.lib.sq_jk_prim(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs),
+                                          ctypes.byref(self.slots), ctypes.byref(qs), ptr(self.tab64), ptr(self.tab32),
+                                          ptr(D), ptr(Jacc), ptr(Kacc), float(prim_tau), s.cuda_stream), "sq_jk_prim")
+                continue
             check(self.lib.sq_jk(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(self.slots),
                                  ctypes.byref(qs), ptr(self.tab64), ptr(self.tab32), ptr(D), ptr(D32), ptr(Jacc),
                                  ptr(Kacc), _lib.PRECISIONS[prec], s.cuda_stream), "sq_jk")
@@ -737,10 +753,16 @@ class IntegralEngine:
         "fp64": every quartet FP64; "mixed": quartets with bound < fp32_threshold
         in FP32 (FP64 Boys recursion); "mixed_boys32": the same, recursion in FP32
         too; "mixed_chunk": the "mixed" test applied per bra primitive chunk of
-        the large-bound quartets (classes with per-thread kernels).
+        the large-bound quartets (classes with per-thread kernels);
+        "mixed_prim": the "mixed" lists, with the large-bound quartets' primitive
+        quartets of bound q_ij q_kl < fp32_threshold run in FP32 inside the FP64
+        launch (sq_jk_prim).
         """
         if precision == "fp64":
             return [self.quartets(threshold)], ["fp64"]
+        if precision == "mixed_prim":
+            q64, q32 = self.quartets(threshold, fp32_threshold)
+            return [q64, q32], ["fp64_prim", "fp32"]
         if precision not in ("mixed", "mixed_boys32", "mixed_chunk"):
             raise ValueError(f"unknown precision {precision!r}")
         q64, q32 = self.quartets(threshold, fp32_threshold, chunks=precision == "mixed_chunk")
@@ -750,6 +772,8 @@ class IntegralEngine:
                  fp32_threshold: float = 1e-4):
         """J_i, K_i (symmetrised, [nd, nbf, nbf]) for a stack of densities Ds [nd, nbf, nbf],
         with each quartet's integrals evaluated once for all of them (sq_jk_multi)."""
+        if precision == "mixed_prim":
+            raise ValueError("precision 'mixed_prim' serves one density per call (use 'mixed' for several)")
         lists, precs = self._lists_for(precision, threshold, fp32_threshold)
         Ds = Ds.to(device=self.device, dtype=torch.float64).contiguous()
         nd = Ds.shape[0]
@@ -772,10 +796,11 @@ class IntegralEngine:
         """Coulomb and exchange matrices J, K (symmetrised) for density D.
 
         precision: "fp64" (every quartet FP64), "mixed" (bound < fp32_threshold
-        in FP32 with FP64 Boys), "mixed_boys32" (those quartets fully FP32).
+        in FP32 with FP64 Boys), "mixed_boys32" (those quartets fully FP32),
+        "mixed_chunk" and "mixed_prim" (the same test at finer grain, see _lists_for).
         """
         lists, precs = self._lists_for(precision, threshold, fp32_threshold)
-        Jacc, Kacc = self.jk_accumulate(D, lists, precs)
+        Jacc, Kacc = self.jk_accumulate(D, lists, precs, prim_tau=fp32_threshold)
         J = torch.empty_like(Jacc)
         K = torch.empty_like(Kacc)
         check(self.lib.sq_fock_build(self.nbf, None, ptr(Jacc), ptr(Kacc), None, ptr(J), ptr(K), self._stream()),
@@ -786,7 +811,7 @@ class IntegralEngine:
              fp32_threshold: float = 1e-4) -> torch.Tensor:
         """F = H + J - K/2 built directly from screened ERIs."""
         lists, precs = self._lists_for(precision, threshold, fp32_threshold)
-        Jacc, Kacc = self.jk_accumulate(D, lists, precs)
+        Jacc, Kacc = self.jk_accumulate(D, lists, precs, prim_tau=fp32_threshold)
         F = torch.empty_like(Jacc)
         check(self.lib.sq_fock_build(self.nbf, ptr(H.contiguous()), ptr(Jacc), ptr(Kacc), ptr(F), None, None,
                                      self._stream()), "sq_fock_build")

@@ -67,7 +67,9 @@ class DirectJK:
     """Integral-direct J/K callable for run_hartree_fock.
 
     precision: "fp64", "mixed" (quartets with Schwarz bound < fp32_threshold in
-    FP32 with FP64 Boys recursion) or "mixed_boys32".  In mixed modes the SCF
+    FP32 with FP64 Boys recursion), "mixed_boys32", "mixed_chunk" or
+    "mixed_prim" (the bound test per primitive quartet inside the large-bound
+    quartets, see IntegralEngine._lists_for).  In mixed modes the SCF
     switches to FP64 once the DIIS error max|FDS - SDF| drops below
     ``fp64_tail_diis_error`` (call ``switch_to_fp64``).
     """
