@@ -403,3 +403,26 @@ def test_headline_fixtures_match_the_synthetic_generators():
         # the SCF converged: the last two iteration energies agree to the SCF threshold
         assert abs(g["energies"][-1] - g["energies"][-2]) < 1e-9
         assert abs(float(g["E_at_D"]) - float(g["E_hf"])) < 1e-9
+
+
+def test_dropin_aliases_resolve_and_uninstall_cleanly():
+    """Option A: the reference's module names import this package's objects; uninstall restores sys.modules."""
+    import sys
+
+    from slowquant_gb300 import dropin, hartreefock
+
+    before = {k: v for k, v in sys.modules.items() if k == "slowquant" or k.startswith("slowquant.")}
+    saved = dropin.install()
+    try:
+        import slowquant.SlowQuant as sq
+        from slowquant.hartreefock.diis import DIIS
+        from slowquant.hartreefock.hartreefock_in_memory import run_hartree_fock
+        from slowquant.molecularintegrals.electronrepulsion import get_cauchy_schwarz_matrix  # noqa: F401
+        from slowquant.molecularintegrals.integralclass import _Integral  # noqa: F401
+
+        assert sq.SlowQuant.__module__ == "slowquant_gb300.SlowQuant"
+        assert DIIS is hartreefock.DIIS and run_hartree_fock is hartreefock.run_hartree_fock
+    finally:
+        dropin.uninstall(saved)
+    after = {k: v for k, v in sys.modules.items() if k == "slowquant" or k.startswith("slowquant.")}
+    assert after == before
