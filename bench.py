@@ -319,6 +319,8 @@ def gpu_arm(args) -> None:
     lib = _lib.lib()
     if args.jk_streams:
         _lib.check(lib.sq_set_option(_lib.SQ_OPT_JK_STREAMS, args.jk_streams), "sq_set_option")
+    if args.warp_below is not None:
+        _lib.check(lib.sq_set_option(_lib.SQ_OPT_WARP_BELOW, args.warp_below), "sq_set_option")
 
     geom = workload_geometry()
     mol = _Molecule(geom, 0, "angstrom")
@@ -523,6 +525,7 @@ def gpu_arm(args) -> None:
         "wall_timed_s": round(wall_mixed, 3),
         "hbm_peak_gbs": measured_peaks().get("hbm_gbs"),
         "jk_streams": int(lib.sq_get_option(_lib.SQ_OPT_JK_STREAMS)),
+        "warp_below": int(lib.sq_get_option(_lib.SQ_OPT_WARP_BELOW)),
     }
     if rank == 0 and not args.no_cpu:
         pairs_host = (eng.pair_shells[eng.slot_pair], q_all.pairs[: q_all.nquartet].cpu().numpy())
@@ -575,24 +578,36 @@ def batch_arm(args) -> None:
     t0 = time.time()
     tuning = BatchSCF(be, "mixed").autotune()
     tune_s = time.time() - t0
+    steps = max(1, min(args.steps, 3))
+
+    def timed_runs(scf):
+        scf.run()  # warm-up run: captures the iteration graphs, which later runs replay
+        torch.cuda.synchronize()
+        t0 = time.time()
+        for _ in range(steps):
+            E = scf.run()
+        torch.cuda.synchronize()
+        return E, (time.time() - t0) / steps
+
     for prec in ("fp64", "mixed"):
         t0 = time.time()
         scf = BatchSCF(be, prec)
         torch.cuda.synchronize()
         prep_s = time.time() - t0
-        E = scf.run()  # warm-up run: captures the Fock-build graphs
-        steps = max(1, min(args.steps, 3))
-        t0 = time.time()
-        for _ in range(steps):
-            scf = BatchSCF(be, prec)
-            scf.graphs = {}
-            E = scf.run()
-        torch.cuda.synchronize()
-        scf_s = (time.time() - t0) / steps
+        E, scf_s = timed_runs(scf)
         mode = "fp64" if prec == "fp64" else "mixed"
         ms_fock = float(np.median(time_events(torch, lambda: scf.fock(mode), 5)))
-        res[prec] = {"molecules_per_s": len(mols) / scf_s, "scf_s": scf_s, "iterations": scf.iterations,
-                     "fock_build_ms": ms_fock, "list_prep_s": round(prep_s, 2), "E": E}
+        # the same SCF with the built-in launch shapes, and with eager iterations (no graphs)
+        autotune.reset()
+        _, scf_default_s = timed_runs(BatchSCF(be, prec))
+        _, scf_eager_s = timed_runs(BatchSCF(be, prec, use_graphs=False))
+        autotune.apply(tuning)
+        res[prec] = {"molecules_per_s": len(mols) / scf_s, "scf_s": scf_s,
+                     "per_molecule_scf_ms": scf_s * 1e3 / len(mols), "iterations": scf.iterations,
+                     "host_syncs_per_scf": scf.host_syncs, "fock_build_ms": ms_fock,
+                     "molecules_per_s_default_launch_shapes": len(mols) / scf_default_s,
+                     "molecules_per_s_eager_iterations": len(mols) / scf_eager_s,
+                     "list_prep_s": round(prep_s, 2), "E": E}
     dE = float(np.max(np.abs(res["mixed"]["E"] - res["fp64"]["E"])))
     for r in res.values():
         r.pop("E")
@@ -603,7 +618,8 @@ def batch_arm(args) -> None:
         "vs_baseline": None, "dtype": "f64+f32 (mixed)", "data": "synthetic",
         "config": {"workload": f"{len(mols)} water clusters (H2O)_k, k~U{{1..6}} (seed 256), 6-31G*, full RHF SCF",
                    "total_bf": int(sum(m.number_bf for m in mols)), "waters": int(sizes.sum()),
-                   "step": "one batched SCF to convergence (dE, rmsD < 1e-9) of every molecule"},
+                   "step": "one batched SCF to convergence (dE, rmsD < 1e-9) of every molecule, each iteration "
+                           "replayed from a CUDA graph"},
         "fp64": res["fp64"], "mixed": res["mixed"], "max_abs_dE_mixed_vs_fp64": dE,
         "setup_s": round(setup_s, 2), "autotune_s": round(tune_s, 2),
         "launch_shapes": {f"{c}:{p}": [t, b] for (c, p), (t, b, _) in sorted(tuning.items()) if t},
@@ -681,6 +697,8 @@ def main() -> None:
                     help="fock: the headline Fock-build line; batch / gradient: secondary measurements")
     ap.add_argument("--batch-size", type=int, default=256)
     ap.add_argument("--jk-streams", type=int, default=0, help="J/K class launch streams (0: library default)")
+    ap.add_argument("--warp-below", type=int, default=None,
+                    help="classes 12-18: launches with fewer quartets run on the warp kernel (library default)")
     ap.add_argument("--tau-sweep", type=float, nargs="*", default=[1e-5, 1e-4, 1e-3, 1e-2, 1e-1],
                     help="FP32 Schwarz thresholds reported beside the headline (empty: skip)")
     ap.add_argument("--prim-sweep", type=float, nargs="*", default=[1e-4, 1e-3, 1e-2],

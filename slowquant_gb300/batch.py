@@ -392,59 +392,85 @@ def batched_eigh(M: torch.Tensor, tol: float = 1e-15, max_sweeps: int = 40):
 
 
 class _BatchDIIS:
-    """Pulay DIIS (diis.py:4-66 semantics) for a [count, n, n] group, ring buffer of 6."""
+    """Pulay DIIS (diis.py:4-66 semantics) for a [count, n, n] group, entirely on the device.
+
+    The six stored (F, error) pairs live in a ring buffer whose write position
+    and fill count are device tensors, and the bordered system always has the
+    full 7 x 7 shape: a slot not yet written gets a unit diagonal and a zero
+    border, so its coefficient is 0.  The coefficients solve the same system
+    as the reference's (the order of the stored vectors does not change the
+    solution), one vector gives c = 1 (F unchanged, as the reference's first
+    call), and nothing depends on host state, so a whole SCF iteration can be
+    captured in a CUDA graph and replayed.  Blocks of 2 functions skip DIIS,
+    as the reference does.
+    """
 
     def __init__(self, count: int, n: int, device, nsave: int = 6):
+        self.n = n
+        self.nsave = nsave
         self.F = torch.zeros((nsave, count, n, n), dtype=torch.float64, device=device)
         self.E = torch.zeros_like(self.F)
-        self.nsave = nsave
-        self.k = 0  # vectors stored
-        self.head = 0
-        self.last_error = None
+        self.head = torch.zeros(1, dtype=torch.int64, device=device)
+        self.k = torch.zeros(1, dtype=torch.int64, device=device)
+        self.slots = torch.arange(nsave, device=device)
+        self.last_error = torch.zeros(count, dtype=torch.float64, device=device)
+
+    def reset(self) -> None:
+        self.head.zero_()
+        self.k.zero_()
 
     def extrapolate(self, F, D, S):
-        if F.shape[-1] == 2:
+        if self.n == 2:
             return F
         err = F @ D @ S - S @ D @ F
-        self.last_error = err.abs().amax(dim=(1, 2))
-        self.F[self.head] = F
-        self.E[self.head] = err
-        self.head = (self.head + 1) % self.nsave
-        self.k = min(self.k + 1, self.nsave)
-        if self.k == 1:
-            return F
-        # keep the reference's oldest-first order of the stored vectors
-        idx = [(self.head - self.k + i) % self.nsave for i in range(self.k)]
-        Es = self.E[idx]  # [k, count, n, n]
-        Fs = self.F[idx]
-        m = self.k
-        Bm = torch.einsum("icpq,jcqp->cij", Es, Es)
+        self.last_error.copy_(err.abs().amax(dim=(1, 2)))
+        self.F.index_copy_(0, self.head, F[None])
+        self.E.index_copy_(0, self.head, err[None])
+        self.head.copy_(torch.remainder(self.head + 1, self.nsave))
+        self.k.copy_(torch.clamp(self.k + 1, max=self.nsave))
+        valid = self.slots < self.k  # slots are written 0, 1, 2, ... then reused
+        m = self.nsave
+        Bm = torch.einsum("icpq,jcqp->cij", self.E, self.E)
+        pair = valid[:, None] & valid[None, :]
+        Bm = torch.where(pair, Bm, torch.zeros_like(Bm)) + torch.diag_embed((~valid).to(Bm.dtype)).expand_as(Bm)
         count = F.shape[0]
+        border = torch.where(valid, -1.0, 0.0).to(torch.float64)
         B = torch.zeros((count, m + 1, m + 1), dtype=torch.float64, device=F.device)
-        B[:, -1, :] = -1
-        B[:, :, -1] = -1
-        B[:, -1, -1] = 0
         B[:, :m, :m] = Bm
+        B[:, m, :m] = border
+        B[:, :m, m] = border
         b0 = torch.zeros((count, m + 1), dtype=torch.float64, device=F.device)
-        b0[:, -1] = -1
-        # solve_ex: no singularity check, so no host synchronisation per group
+        b0[:, m] = -1
+        # solve_ex: no singularity check, so no host synchronisation
         c = torch.linalg.solve_ex(B, b0)[0]
-        return torch.einsum("ci,icpq->cpq", c[:, :m], Fs)
+        return torch.einsum("ci,icpq->cpq", c[:, :m], self.F)
 
 
 class BatchSCF:
     """Restricted HF of every molecule of a BatchEngine (hartreefock_in_memory.py:7-94 semantics,
     batched per size group).  precision: "fp64" or "mixed" (FP32 quartets below fp32_threshold
-    until every molecule's DIIS error is below fp64_tail_diis_error, then FP64)."""
+    until every molecule's DIIS error is below fp64_tail_diis_error, then FP64).
+
+    With ``use_graphs`` (default) a whole SCF iteration -- the Fock build, DIIS,
+    the orthogonalised eigensolve, the new density, the energies and the
+    convergence test -- is captured once per precision in a CUDA graph and
+    replayed.  Convergence is a device flag: once every molecule meets the
+    thresholds the state stops changing, so the host reads the flag only every
+    ``check_every`` iterations and the results equal stopping at the converged
+    iteration.  In mixed precision the host reads the FP64-switch test every
+    iteration until the switch.
+    """
 
     def __init__(self, be: BatchEngine, precision: str = "fp64", threshold: float = 1e-12,
-                 fp32_threshold: float = 1e-4, fp64_tail_diis_error: float = 1e-5, use_graphs: bool = True):
+                 fp32_threshold: float = 1e-4, fp64_tail_diis_error: float = 1e-5, use_graphs: bool = True,
+                 check_every: int = 4):
         self.be = be
         self.precision = precision
         self.threshold = threshold
         self.fp32_threshold = fp32_threshold
         self.tail = fp64_tail_diis_error
         self.use_graphs = use_graphs
+        self.check_every = max(1, int(check_every))
         dev = be.device
         tot = be.mat_total
         self.S, T, V = be.one_electron()
@@ -461,6 +487,7 @@ class BatchSCF:
         self.graphs: dict = {}
         self.builds: list[str] = []
         self.tuning: dict = {}
+        self.host_syncs = 0
 
     def autotune(self, threads=None, waves=None) -> dict:
         """Pick each quartet class's launch shape (threads per block, grid cap) for this
@@ -485,6 +512,7 @@ class BatchSCF:
             table.update(autotune.tune(run_class, lists, precs, **kw))
         self.tuning = table
         self.graphs = {}  # re-capture with the tuned shapes
+        self.fock_graphs = {}
         return table
 
     def _fock_into_F(self, mode: str) -> None:
@@ -498,12 +526,14 @@ class BatchSCF:
             F.copy_(be.view(self.H, g) + 0.5 * (J + J.transpose(1, 2)) - 0.25 * (K + K.transpose(1, 2)))
 
     def fock(self, mode: str) -> None:
-        """F <- H + J(D) - K(D)/2 for the whole batch (replayed from a CUDA graph)."""
-        self.builds.append(mode)
+        """F <- H + J(D) - K(D)/2 for the whole batch alone (replayed from its own CUDA graph);
+        the SCF iterations capture the build inside their iteration graphs instead."""
         if not self.use_graphs:
             self._fock_into_F(mode)
             return
-        if mode not in self.graphs:
+        if not hasattr(self, "fock_graphs"):
+            self.fock_graphs = {}
+        if mode not in self.fock_graphs:
             # warm up on a side stream, then capture the build once
             s = torch.cuda.Stream(self.be.device)
             s.wait_stream(torch.cuda.current_stream(self.be.device))
@@ -513,8 +543,8 @@ class BatchSCF:
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g):
                 self._fock_into_F(mode)
-            self.graphs[mode] = g
-        self.graphs[mode].replay()
+            self.fock_graphs[mode] = g
+        self.fock_graphs[mode].replay()
 
     def _eigh_all(self, A_flat: torch.Tensor):
         """Eigenvectors of every molecule's block of a packed buffer in one launch (sq_batched_eigh).
@@ -544,67 +574,127 @@ class BatchSCF:
                                          ptr(woffs), 1e-14, 40, None, _lib.stream_handle()), "sq_batched_eigh")
         return V
 
-    def run(self, dE_threshold: float = 1e-9, rmsd_threshold: float = 1e-9, max_iter: int = 100):
+    def _setup_state(self) -> None:
+        """Core-Hamiltonian guess and the per-group state (hartreefock_in_memory.py:30-42).
+
+        A second run of the same object writes into the first run's tensors,
+        so the iteration graphs captured then stay valid and are replayed."""
         be = self.be
-        X, Hs, Ss, diis, E0, nocc, U = [], [], [], [], [], [], []
-        for g in be.groups:
+        first = not hasattr(self, "X")
+        if first:
+            self.X, self.U, self.E, self.diis, self.nocc = [], [], [], [], []
+        for gi, g in enumerate(be.groups):
             S = be.view(self.S, g)
             H = be.view(self.H, g)
             lam, L = batched_eigh(S)
             Xg = L @ torch.diag_embed(lam ** (-0.5)) @ L.transpose(1, 2)
             _, C0p = batched_eigh(Xg.transpose(1, 2) @ H @ Xg.transpose(1, 2))
             C0 = Xg @ C0p
-            U.append(C0p)
             Co = C0[:, :, : g.nocc]
             be.view(self.D, g).copy_(2 * Co @ Co.transpose(1, 2))
-            E0.append(torch.sum(be.view(self.D, g) * H, dim=(1, 2)))
-            X.append(Xg)
-            Hs.append(H)
-            Ss.append(S)
-            diis.append(_BatchDIIS(len(g.mols), g.nbf, be.device))
-            nocc.append(g.nocc)
+            E0 = torch.sum(be.view(self.D, g) * H, dim=(1, 2))
+            if first:
+                self.E.append(E0)
+                self.X.append(Xg)
+                self.U.append(C0p.contiguous())
+                self.diis.append(_BatchDIIS(len(g.mols), g.nbf, be.device))
+                self.nocc.append(g.nocc)
+            else:
+                self.E[gi].copy_(E0)
+                self.X[gi].copy_(Xg)
+                self.U[gi].copy_(C0p)
+                self.diis[gi].reset()
+        if first:
+            dev = be.device
+            self.Fp = torch.zeros_like(self.F)  # packed orthogonalised Fock matrices
+            self.done = torch.zeros(1, dtype=torch.bool, device=dev)
+            self.tail_ok = torch.zeros(1, dtype=torch.bool, device=dev)
+            self.iters = torch.zeros(1, dtype=torch.int64, device=dev)
+        else:
+            self.done.zero_()
+            self.tail_ok.zero_()
+            self.iters.zero_()
+
+    def _iterate(self, mode: str, dE_threshold: float, rmsd_threshold: float) -> None:
+        """One SCF iteration of every molecule, device work only (graph-capturable)."""
+        be = self.be
+        self._fock_into_F(mode)
+        Fx = []
+        for gi, g in enumerate(be.groups):
+            F = self.diis[gi].extrapolate(be.view(self.F, g).clone(), be.view(self.D, g).clone(),
+                                          be.view(self.S, g))
+            Fx.append(F)
+            # in the previous iteration's orbital basis U the Fock matrix is nearly
+            # diagonal, so the Jacobi sweeps converge in a few sweeps
+            XU = self.X[gi] @ self.U[gi]
+            be.view(self.Fp, g).copy_(XU.transpose(1, 2) @ F @ XU)
+        V = self._eigh_all(self.Fp)  # one eigensolver launch for all molecules
+        live = ~self.done
+        conv = torch.ones(1, dtype=torch.bool, device=be.device)
+        tail = torch.ones(1, dtype=torch.bool, device=be.device)
+        for gi, g in enumerate(be.groups):
+            Un = self.U[gi] @ be.view(V, g)
+            C = self.X[gi] @ Un
+            Co = C[:, :, : self.nocc[gi]]
+            Dn = 2 * Co @ Co.transpose(1, 2)
+            Dv = be.view(self.D, g)
+            En = 0.5 * torch.sum(Dn * (be.view(self.H, g) + Fx[gi]), dim=(1, 2))
+            dE = (En - self.E[gi]).abs().amax()
+            rmsd = torch.sqrt(torch.sum((Dn - Dv) ** 2, dim=(1, 2))).amax()
+            conv = conv & (dE < dE_threshold) & (rmsd < rmsd_threshold)
+            tail = tail & (self.diis[gi].last_error.amax() < self.tail)
+            # a converged batch keeps its state: later replays change nothing
+            self.U[gi].copy_(torch.where(live, Un, self.U[gi]))
+            Dv.copy_(torch.where(live, Dn, Dv))
+            self.E[gi].copy_(torch.where(live, En, self.E[gi]))
+        self.iters.add_(live.to(torch.int64))
+        self.tail_ok.copy_(tail)
+        if mode == "fp64":  # the mixed phase never stops: it ends with the switch to FP64
+            self.done.copy_(self.done | conv)
+
+    def _step(self, mode: str, dE_threshold: float, rmsd_threshold: float) -> None:
+        self.builds.append(mode)
+        if not self.use_graphs:
+            self._iterate(mode, dE_threshold, rmsd_threshold)
+            return
+        if mode not in self.graphs:
+            # the first iteration in this precision runs on a side stream (warming up
+            # every library handle), then the iteration is captured once
+            s = torch.cuda.Stream(self.be.device)
+            s.wait_stream(torch.cuda.current_stream(self.be.device))
+            with torch.cuda.stream(s):
+                self._iterate(mode, dE_threshold, rmsd_threshold)
+            torch.cuda.current_stream(self.be.device).wait_stream(s)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                self._iterate(mode, dE_threshold, rmsd_threshold)
+            self.graphs[mode] = g
+            return
+        self.graphs[mode].replay()
+
+    def run(self, dE_threshold: float = 1e-9, rmsd_threshold: float = 1e-9, max_iter: int = 100):
+        be = self.be
+        self._setup_state()
         mode = "fp64" if self.precision == "fp64" else "mixed"
-        E = E0
-        self.iterations = 0
-        Fp = torch.zeros_like(self.F)  # packed S^-1/2 F S^-1/2 of every molecule
-        Fx = [None] * len(be.groups)
-        ng = len(be.groups)
+        self.host_syncs = 0
         for it in range(1, max_iter + 1):
-            self.iterations = it
-            self.fock(mode)
-            # per size group: DIIS and the orthogonal-basis Fock matrix
-            for gi, g in enumerate(be.groups):
-                F = diis[gi].extrapolate(be.view(self.F, g).clone(), be.view(self.D, g).clone(), Ss[gi])
-                Fx[gi] = F
-                # in the previous iteration's orbital basis U the Fock matrix is nearly
-                # diagonal, so the Jacobi sweeps converge in a few sweeps
-                XU = X[gi] @ U[gi]
-                be.view(Fp, g).copy_(XU.transpose(1, 2) @ F @ XU)
-            # one eigensolver launch for all molecules
-            V = self._eigh_all(Fp)
-            stats = torch.zeros((ng, 3), dtype=torch.float64, device=be.device)
-            newE = []
-            for gi, g in enumerate(be.groups):
-                U[gi] = U[gi] @ be.view(V, g)
-                C = X[gi] @ U[gi]
-                Co = C[:, :, : nocc[gi]]
-                Dn = 2 * Co @ Co.transpose(1, 2)
-                En = 0.5 * torch.sum(Dn * (Hs[gi] + Fx[gi]), dim=(1, 2))
-                stats[gi, 0] = (En - E[gi]).abs().max()
-                stats[gi, 1] = torch.sqrt(torch.sum((Dn - be.view(self.D, g)) ** 2, dim=(1, 2))).max()
-                if diis[gi].last_error is not None:  # None: DIIS is off for 2-function molecules
-                    stats[gi, 2] = diis[gi].last_error.max()
-                be.view(self.D, g).copy_(Dn)
-                newE.append(En)
-            E = newE
-            st = stats.cpu().numpy()  # the one host synchronisation of the iteration
-            conv_all = bool(np.all(st[:, 0] < dE_threshold) and np.all(st[:, 1] < rmsd_threshold))
-            if mode == "mixed" and bool(np.all(st[:, 2] < self.tail)):
-                mode = "fp64"
-                diis = [_BatchDIIS(len(g.mols), g.nbf, be.device) for g in be.groups]
-                conv_all = False
-            if conv_all and mode == "fp64":
-                break
+            self._step(mode, dE_threshold, rmsd_threshold)
+            if mode == "mixed":
+                self.host_syncs += 1
+                if bool(self.tail_ok.item()):
+                    mode = "fp64"
+                    for d in self.diis:
+                        d.reset()
+            elif it % self.check_every == 0 or it == max_iter:
+                self.host_syncs += 1
+                if bool(self.done.item()):
+                    break
+        self.iterations = int(self.iters.item())
+        if not bool(self.done.item()):
+            import warnings
+
+            warnings.warn(f"batched RHF did not converge in {max_iter} iterations", stacklevel=2)
+        E = self.E
         # energies back in the caller's molecule order
         Eb = torch.cat(E).cpu().numpy()
         out = np.empty(be.nmol)

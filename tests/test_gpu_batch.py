@@ -149,3 +149,25 @@ def test_batch_of_one_molecule(gpu_lib):
     mols = _mols([2])
     E = BatchSCF(BatchEngine(mols), "fp64").run(1e-10, 1e-10)
     np.testing.assert_allclose(E, [_single_energy(mols[0])], atol=1e-8)
+
+
+def test_captured_iterations_replay_and_match_eager_iterations(gpu_lib):
+    """Whole SCF iterations replayed from CUDA graphs give the eager iterations' energies and
+    iteration counts; a second run replays the first run's graphs; the host reads the
+    convergence flag only every few iterations."""
+    from slowquant_gb300.batch import BatchEngine, BatchSCF
+
+    be = BatchEngine(_mols([2, 1, 3, 2]))
+    for prec in ("fp64", "mixed"):
+        eager = BatchSCF(be, prec, use_graphs=False)
+        E_eager = eager.run()
+        scf = BatchSCF(be, prec, check_every=4)
+        E1 = scf.run()
+        graphs = dict(scf.graphs)
+        E2 = scf.run()
+        np.testing.assert_allclose(E1, E_eager, atol=1e-10)
+        np.testing.assert_allclose(E2, E1, atol=1e-12)
+        assert scf.iterations == eager.iterations
+        assert all(scf.graphs[k] is graphs[k] for k in graphs)  # replayed, not captured again
+        if prec == "fp64":
+            assert scf.host_syncs < scf.iterations
