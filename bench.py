@@ -319,8 +319,6 @@ def gpu_arm(args) -> None:
     lib = _lib.lib()
     if args.jk_streams:
         _lib.check(lib.sq_set_option(_lib.SQ_OPT_JK_STREAMS, args.jk_streams), "sq_set_option")
-    if args.warp_below is not None:
-        _lib.check(lib.sq_set_option(_lib.SQ_OPT_WARP_BELOW, args.warp_below), "sq_set_option")
 
     geom = workload_geometry()
     mol = _Molecule(geom, 0, "angstrom")
@@ -439,7 +437,9 @@ def gpu_arm(args) -> None:
     prim_modes = []
     for tau in args.prim_sweep:
         eng.fock(H, D, SCREEN, "mixed_prim", tau)
+        torch.cuda.nvtx.range_push(f"timed_prim_{tau:g}")
         ms_p = float(np.median(time_events(torch, lambda: eng.fock(H, D, SCREEN, "mixed_prim", tau), 5, flush)))
+        torch.cuda.nvtx.range_pop()
         Fp = eng.fock(H, D, SCREEN, "mixed_prim", tau)
         jkp = DirectJK(eng, SCREEN, "mixed_prim", tau, 1e-5)
         Ep, _, _, _ = run_hartree_fock(S, T, V, jkp, ne, log, 1e-9, 1e-9, 100, True)
@@ -525,7 +525,6 @@ def gpu_arm(args) -> None:
         "wall_timed_s": round(wall_mixed, 3),
         "hbm_peak_gbs": measured_peaks().get("hbm_gbs"),
         "jk_streams": int(lib.sq_get_option(_lib.SQ_OPT_JK_STREAMS)),
-        "warp_below": int(lib.sq_get_option(_lib.SQ_OPT_WARP_BELOW)),
     }
     if rank == 0 and not args.no_cpu:
         pairs_host = (eng.pair_shells[eng.slot_pair], q_all.pairs[: q_all.nquartet].cpu().numpy())
@@ -697,8 +696,6 @@ def main() -> None:
                     help="fock: the headline Fock-build line; batch / gradient: secondary measurements")
     ap.add_argument("--batch-size", type=int, default=256)
     ap.add_argument("--jk-streams", type=int, default=0, help="J/K class launch streams (0: library default)")
-    ap.add_argument("--warp-below", type=int, default=None,
-                    help="classes 12-18: launches with fewer quartets run on the warp kernel (library default)")
     ap.add_argument("--tau-sweep", type=float, nargs="*", default=[1e-5, 1e-4, 1e-3, 1e-2, 1e-1],
                     help="FP32 Schwarz thresholds reported beside the headline (empty: skip)")
     ap.add_argument("--prim-sweep", type=float, nargs="*", default=[1e-4, 1e-3, 1e-2],

@@ -203,11 +203,6 @@ const char *sq_last_error(void);
  * ((ss|ss), (ps|ss), (ps|ps), (pp|ss), (pp|ps), (ds|ss), (ds|ps), (dp|ss))
  * one quartet per thread, 0 one quartet per warp like the other classes. */
 #define SQ_OPT_GRAD_THREAD 4
-/* SQ_OPT_WARP_BELOW: a J/K launch of classes 12-18 with fewer quartets than
- * this runs on the generic warp kernel instead of its per-thread kernel (one
- * thread per whole quartet makes a short launch as long as one quartet's
- * serial work).  -1 (default): 2 x SMs x 128; 0 keeps the per-thread kernels. */
-#define SQ_OPT_WARP_BELOW 5
 int sq_set_option(int key, long long value);
 long long sq_get_option(int key);
 

@@ -39,7 +39,6 @@ SQ_OPT_GENERIC_MIN_L = 1
 SQ_OPT_JK_STREAMS = 2
 SQ_OPT_FP64_UNROLLED_HIGH = 3
 SQ_OPT_GRAD_THREAD = 4
-SQ_OPT_WARP_BELOW = 5
 SQ_NOALLOC_MAX_NBF = 1024
 SQ_NOALLOC_MAX_ELEMS = SQ_NOALLOC_MAX_NBF * SQ_NOALLOC_MAX_NBF
 

@@ -93,12 +93,6 @@ static int g_generic_min_l = 5;
 // Bit c set: the FP64 J/K launches of class c run on its kLaunchersF64 kernel,
 // else on the warp kernel (option SQ_OPT_FP64_UNROLLED_HIGH).
 static long long g_fp64_unrolled_high = 0x7FLL << 12;  // classes 12-18
-// The per-thread kernels of classes 12-18 give each thread a whole (dp|pp) ...
-// (dd|ds) quartet: a launch of few quartets lasts as long as one thread's
-// serial work.  Launches of fewer than this many quartets run on the warp
-// kernel (32 lanes per quartet) instead (option SQ_OPT_WARP_BELOW; -1: twice
-// the SM count times 128).  Both kernels number sub-slot chunks alike.
-static long long g_warp_below = -1;
 // Per-thread gradient kernels for the light classes (option SQ_OPT_GRAD_THREAD).
 static int g_grad_thread = 1;
 int grad_thread_enabled() { return g_grad_thread; }
@@ -195,10 +189,6 @@ static cudaError_t launch_class(EriArgs &args, const sq_quartets *qs, int c, int
     const int plain = precision == SQ_FP64_PRIM ? SQ_FP64 : precision;
     if (mode == MODE_JK && precision == SQ_FP64_PRIM && L < g_generic_min_l && kLaunchers[c] != nullptr)
         return kLaunchers[c](args, mode, precision, stream);
-    const bool heavy = unrolled != nullptr && (unrolled == kLaunchersF64[c] || unrolled == kLaunchersF32[c]);
-    const long long below = g_warp_below >= 0 ? g_warp_below : 2 * sm_count() * 128;
-    if (heavy && warp_fits && args.nq < below)
-        return launch_eri_warp(args, WarpClass{la, lb, lc, ld}, mode, plain, stream);
     if (unrolled != nullptr) return unrolled(args, mode, plain, stream);
     if (!warp_fits) return launch_eri_block(args, la, lb, lc, ld, mode, plain, stream);
     return launch_eri_warp(args, WarpClass{la, lb, lc, ld}, mode, plain, stream);
@@ -274,11 +264,6 @@ extern "C" int sq_set_option(int key, long long value) {
         g_fp64_unrolled_high = value;
         return SQ_OK;
     }
-    if (key == SQ_OPT_WARP_BELOW) {
-        if (value < -1) return set_error(SQ_ERR_ARG, "sq_set_option: quartet count below -1");
-        g_warp_below = value;
-        return SQ_OK;
-    }
     if (key == SQ_OPT_GENERIC_MIN_L) {
         if (value < 0) return set_error(SQ_ERR_ARG, "sq_set_option: negative L");
         g_generic_min_l = (int)value;
@@ -301,7 +286,6 @@ extern "C" long long sq_get_option(int key) {
     if (key == SQ_OPT_JK_STREAMS) return g_jk_streams;
     if (key == SQ_OPT_FP64_UNROLLED_HIGH) return g_fp64_unrolled_high;
     if (key == SQ_OPT_GRAD_THREAD) return g_grad_thread;
-    if (key == SQ_OPT_WARP_BELOW) return g_warp_below;
     return -1;
 }
 

@@ -118,66 +118,41 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
         const int2 pq = args.quartets[qi];
         const int P = args.use_slots ? gload(args.slots.pair + pq.x) : pq.x;
         const int Q = args.use_slots ? gload(args.slots.pair + pq.y) : pq.y;
-        // Primitive-pair data of bra and ket: base of primitive 0 and the
-        // strides to the next primitive / next field (p, Px, Py, Pz, U), and
-        // to the next primitive / next Hermite value.  J/K lists read the slot
-        // layout through the descriptors, so that a sub-slot chunk covers the
-        // same primitive pairs (the slot's kept ones, in descending Schwarz
-        // factor) as in the per-thread kernels and a class may run on either
-        // kernel; dense-tensor and Schwarz lists read the pair table.
-        const R *pB, *pK, *hB, *hK;
-        long long pkB, pfB, hkB, heB, pkK, pfK, hkK, heK;
-        int nbp, nkp;
-        if (MODE == MODE_JK && args.use_slots && args.slots.desc) {
-            const SlotDesc bd = load_desc_prims(args.slots.desc, pq.x), kd = load_desc_prims(args.slots.desc, pq.y);
-            const R *sp = slot_prim_ptr<R>(args.slots);
-            const R *sh = slot_herm_ptr<R>(args.slots);
-            const long long NPP = args.slots.npp_total;
-            pB = sp + bd.pbase, pkB = bd.pstride, pfB = NPP, nbp = bd.npp;
-            hB = sh + bd.hbase, hkB = (long long)EB * bd.pstride, heB = bd.pstride;
-            pK = sp + kd.pbase, pkK = kd.pstride, pfK = NPP, nkp = kd.npp;
-            hK = sh + kd.hbase, hkK = (long long)EK * kd.pstride, heK = kd.pstride;
-        } else {
-            const int i0 = gload(pr.pp_off + P), i1 = gload(pr.pp_off + P + 1);
-            const int k0 = gload(pr.pp_off + Q), k1 = gload(pr.pp_off + Q + 1);
-            // a sub-slot (chunk k of S) covers primitives [k np / S, (k+1) np / S) of its pair
-            int ib0 = i0, ib1 = i1, kb0 = k0, kb1 = k1;
-            if (args.use_slots && args.slots.sub) {
-                const int code = gload(args.slots.sub + pq.x);
-                if (code) {
-                    const int S = code & 0xffff, kc = code >> 16, np = i1 - i0;
-                    ib0 = i0 + (kc * np) / S;
-                    ib1 = i0 + ((kc + 1) * np) / S;
-                }
-                const int codek = gload(args.slots.sub + pq.y);
-                if (codek) {
-                    const int S = codek & 0xffff, kc = codek >> 16, np = k1 - k0;
-                    kb0 = k0 + (kc * np) / S;
-                    kb1 = k0 + ((kc + 1) * np) / S;
-                }
+        const int i0 = gload(pr.pp_off + P), i1 = gload(pr.pp_off + P + 1);
+        const int k0 = gload(pr.pp_off + Q), k1 = gload(pr.pp_off + Q + 1);
+        // a sub-slot (chunk k of S) covers primitives [k np / S, (k+1) np / S) of its pair
+        int ib0 = i0, ib1 = i1, kb0 = k0, kb1 = k1;
+        if (args.use_slots && args.slots.sub) {
+            const int code = gload(args.slots.sub + pq.x);
+            if (code) {
+                const int S = code & 0xffff, kc = code >> 16, np = i1 - i0;
+                ib0 = i0 + (kc * np) / S;
+                ib1 = i0 + ((kc + 1) * np) / S;
             }
-            pB = prim + 8LL * ib0, pkB = 8, pfB = 1, nbp = ib1 - ib0;
-            hB = herm + gload(pr.herm_off + P) + (long long)(ib0 - i0) * EB, hkB = EB, heB = 1;
-            pK = prim + 8LL * kb0, pkK = 8, pfK = 1, nkp = kb1 - kb0;
-            hK = herm + gload(pr.herm_off + Q) + (long long)(kb0 - k0) * EK, hkK = EK, heK = 1;
+            const int codek = gload(args.slots.sub + pq.y);
+            if (codek) {
+                const int S = codek & 0xffff, kc = codek >> 16, np = k1 - k0;
+                kb0 = k0 + (kc * np) / S;
+                kb1 = k0 + ((kc + 1) * np) / S;
+            }
         }
+        const R *hb = herm + gload(pr.herm_off + P);
+        const R *hk = herm + gload(pr.herm_off + Q);
         R acc[KACC];
 #pragma unroll
         for (int k = 0; k < KACC; ++k) acc[k] = R(0);
 
-        for (int i = 0; i < nbp; ++i) {
-            const R *bi = pB + i * pkB;
-            const R p = gload(bi);
-            const R Px = gload(bi + pfB), Py = gload(bi + 2 * pfB), Pz = gload(bi + 3 * pfB);
-            const R Ub = gload(bi + 4 * pfB);
+        for (int i = ib0; i < ib1; ++i) {
+            const R p = gload(prim + 8 * i + 0);
+            const R Px = gload(prim + 8 * i + 1), Py = gload(prim + 8 * i + 2), Pz = gload(prim + 8 * i + 3);
+            const R Ub = gload(prim + 8 * i + 4);
             for (int w = lane; w < NW; w += 32) sm.W[w] = R(0);
-            for (int k = 0; k < nkp; ++k) {
-                const R *kq = pK + k * pkK;
-                const R q = gload(kq);
-                const R X = Px - gload(kq + pfK);
-                const R Y = Py - gload(kq + 2 * pfK);
-                const R Z = Pz - gload(kq + 3 * pfK);
-                const R Uk = gload(kq + 4 * pfK);
+            for (int k = kb0; k < kb1; ++k) {
+                const R q = gload(prim + 8 * k + 0);
+                const R X = Px - gload(prim + 8 * k + 1);
+                const R Y = Py - gload(prim + 8 * k + 2);
+                const R Z = Pz - gload(prim + 8 * k + 3);
+                const R Uk = gload(prim + 8 * k + 4);
                 const R r = rsqrt_r(p + q);
                 const R alpha = p * q * (r * r);
                 const R T = alpha * (X * X + Y * Y + Z * Z);
@@ -260,19 +235,19 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
                     nxt = tmp;
                 }
                 // ket transform
-                const R *ek = hK + k * hkK;
+                const R *ek = hk + (long long)(k - k0) * EK;
                 for (int w = lane; w < NW; w += 32) {
                     const int cd = w / HAB, h = w - cd * HAB;
                     const int tuv = s_tuv[h];
                     const int t = tuv & 255, u = (tuv >> 8) & 255, v = tuv >> 16;
                     const int pw = s_pw_k[cd];
                     const int cx = pw & 255, cy = (pw >> 8) & 255, cz = pw >> 16;
-                    const R *e = ek + s_hoff_k[cd] * heK;
+                    const R *e = ek + s_hoff_k[cd];
                     R s = R(0);
                     for (int tau = 0; tau <= cx; ++tau)
                         for (int nu = 0; nu <= cy; ++nu)
                             for (int phi = 0; phi <= cz; ++phi) {
-                                R ev = gload(e + ((tau * (cy + 1) + nu) * (cz + 1) + phi) * heK);
+                                R ev = gload(e + (tau * (cy + 1) + nu) * (cz + 1) + phi);
                                 if ((tau + nu + phi) & 1) ev = -ev;
                                 s = fma(ev, cur[herm_index(t + tau, u + nu, v + phi)], s);
                             }
@@ -281,7 +256,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
                 __syncwarp();
             }
             // bra transform: lanes own output entries x = lane + 32 kk, x = ab * NCD + cd
-            const R *eb = hB + i * hkB;
+            const R *eb = hb + (long long)(i - i0) * EB;
 #pragma unroll
             for (int kk = 0; kk < KACC; ++kk) {
                 if (kk < kacc) {
@@ -290,13 +265,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) eri_warp_kernel(const Eri
                         const int ab = x / NCD, cd = x - ab * NCD;
                         const int pw = s_pw_b[ab];
                         const int ax = pw & 255, ay = (pw >> 8) & 255, az = pw >> 16;
-                        const R *e = eb + s_hoff_b[ab] * heB;
+                        const R *e = eb + s_hoff_b[ab];
                         R s = R(0);
                         for (int t = 0; t <= ax; ++t)
                             for (int u = 0; u <= ay; ++u)
                                 for (int v = 0; v <= az; ++v)
-                                    s = fma(gload(e + ((t * (ay + 1) + u) * (az + 1) + v) * heB),
-                                            sm.W[herm_index(t, u, v) + HAB * cd], s);
+                                    s = fma(gload(e + (t * (ay + 1) + u) * (az + 1) + v), sm.W[herm_index(t, u, v) + HAB * cd], s);
                         acc[kk] += s;
                     }
                 }

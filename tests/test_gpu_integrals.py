@@ -135,31 +135,6 @@ def test_generic_warp_kernel_matches_per_class_kernels():
             assert np.max(np.abs(K3 - K1)) < 1e-4
 
 
-def test_heavy_classes_on_the_warp_kernel_match_their_per_thread_kernels():
-    """Classes 12-18 routed to the warp kernel (SQ_OPT_WARP_BELOW) give the per-thread results,
-    sub-slot chunks included: both kernels number a slot's primitive pairs alike, so the
-    chunks of one quartet partition it whichever kernel runs them (mixed_chunk places the
-    chunks of one quartet in different lists)."""
-    import torch
-
-    from slowquant_gb300 import _lib, systems
-
-    L = _lib.lib()
-    eng = _engine(systems.water_cluster(3, 6.0, seed=3), "cc-pvdz", "angstrom")
-    D = torch.tensor(_random_density(eng.nbf, 2), dtype=torch.float64, device="cuda")
-    old = L.sq_get_option(_lib.SQ_OPT_WARP_BELOW)
-    try:
-        for prec, tol in (("fp64", 1e-11), ("mixed", 2e-6), ("mixed_chunk", 2e-6), ("mixed_prim", 2e-6)):
-            out = []
-            for below in (0, 10**9):
-                L.sq_set_option(_lib.SQ_OPT_WARP_BELOW, below)
-                out.append([x.cpu().numpy() for x in eng.jk(D, 1e-12, prec, fp32_threshold=1e-3)])
-            np.testing.assert_allclose(out[1][0], out[0][0], atol=tol, err_msg=prec)
-            np.testing.assert_allclose(out[1][1], out[0][1], atol=tol, err_msg=prec)
-    finally:
-        L.sq_set_option(_lib.SQ_OPT_WARP_BELOW, old)
-
-
 def test_driver_entry_points_follow_reference_screening():
     """electronrepulsion.py semantics: no matrix -> all quartets; huge threshold -> zeros."""
     from slowquant_gb300 import electronrepulsion as er

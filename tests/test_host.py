@@ -313,8 +313,6 @@ def test_abi_refuses_bad_arguments_before_touching_the_device():
     try:
         assert defaults[_lib.SQ_OPT_JK_STREAMS] == 8 and defaults[_lib.SQ_OPT_GENERIC_MIN_L] == 5
         assert defaults[_lib.SQ_OPT_FP64_UNROLLED_HIGH] == 0x7F << 12
-        assert L.sq_get_option(_lib.SQ_OPT_WARP_BELOW) == -1
-        assert L.sq_set_option(_lib.SQ_OPT_WARP_BELOW, -2) == _lib.SQ_ERR_ARG
         assert L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, 0) == _lib.SQ_ERR_ARG
         assert L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, 17) == _lib.SQ_ERR_ARG
         assert L.sq_set_option(_lib.SQ_OPT_FP64_UNROLLED_HIGH, 1 << _lib.SQ_MAX_QCLASS) == _lib.SQ_ERR_ARG
