@@ -268,16 +268,22 @@ def reference_arm(args) -> None:
         if step >= args.warmup:
             rates.append(rate)
     value = float(np.median(rates))
+    timings = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "reference_timings.json")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "quartets/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": len(quartets) / value * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": n_step / value * 1e3,
+        "ms_per_step_is": "one timed sample of the workload (the step)",
+        "full_build_ms_extrapolated": len(quartets) / value * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config({"total_quartets": len(quartets)}),
         "cpu_baseline": {"value": value, "unit": "quartets/s", "cores": os.cpu_count() or 1, "kind": "port",
                          "sample": f"per step {n_step} (~{args.cpu_seconds / 2:.0f} s) uniformly random surviving unique shell "
                                    f"quartets of the workload through the oracle's faithful C restatement of "
-                                   f"electron_repulsion_integral (ms_per_step extrapolates to the full "
-                                   f"{len(quartets)}-quartet build)"},
+                                   f"electron_repulsion_integral; full_build_ms_extrapolated scales the rate to "
+                                   f"the {len(quartets)}-quartet build"},
+        "reference_python": json.load(open(timings)) if os.path.exists(timings) else None,
+        "reference_python_is": "the unmodified pure-Python reference timed single-threaded in the build container "
+                               "(tests/golden/time_reference.py); it cannot be installed on the GPU host",
         "e2e": {"value": value, "unit": "quartets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": round(time.time() - t_start, 1),
     }
@@ -485,6 +491,32 @@ def gpu_arm(args) -> None:
     launches = sum(1 for c in range(_lib.SQ_MAX_QCLASS) if q64.class_off[c + 1] > q64.class_off[c]) + sum(
         1 for c in range(_lib.SQ_MAX_QCLASS) if q32.class_off[c + 1] > q32.class_off[c]) + 2
 
+    # the small configurations of the reference timings (tests/golden/reference_timings.json),
+    # through the public facade: ERI tensor and RHF SCF of one water (each the median of 3)
+    small = []
+    for basis in ("sto-3g", "cc-pvdz"):
+        import slowquant_gb300.SlowQuant as sqm
+        from slowquant_gb300 import systems as _sys
+
+        te, ts = [], []
+        for _ in range(3):
+            A = sqm.SlowQuant()
+            A.set_molecule(_sys.water_monomer(), distance_unit="angstrom")
+            A.set_basis_set(basis)
+            torch.cuda.synchronize()
+            t0 = time.time()
+            A.integral.electron_repulsion_tensor
+            torch.cuda.synchronize()
+            te.append(time.time() - t0)
+            A.init_hartree_fock()
+            A.hartree_fock.logger.print_output = False
+            t0 = time.time()
+            A.hartree_fock.run_restricted_hartree_fock()
+            torch.cuda.synchronize()
+            ts.append(time.time() - t0)
+        small.append({"system": "H2O", "basis": basis, "eri_tensor_s": float(np.median(te)),
+                      "scf_s": float(np.median(ts)), "E_hf": A.hartree_fock.E_hf})
+
     clocks = clk.summary()
     line = {
         "metric": METRIC, "value": value, "unit": "quartets/s", "n_gpus": world, "steps": args.steps,
@@ -514,6 +546,7 @@ def gpu_arm(args) -> None:
                      "traffic": None, "flops_per_launch": dom["flops"], "ms_per_launch": dom["ms"]},
         "roofline_fp64_build": {"flops": fl64, "ms": ms64, "achieved_tflops": fl64 / (ms64 * 1e-3) / 1e12,
                                 "peak_tflops": peak64 / 1e12, "frac": fl64 / (ms64 * 1e-3) / peak64},
+        "small_systems": small,
         "tau_sweep": sweep,
         "chunk_precision": chunk_modes,
         "prim_precision": prim_modes,
@@ -529,6 +562,8 @@ def gpu_arm(args) -> None:
     if rank == 0 and not args.no_cpu:
         pairs_host = (eng.pair_shells[eng.slot_pair], q_all.pairs[: q_all.nquartet].cpu().numpy())
         rate, nthreads, n, dt = cpu_sample(None, args.cpu_seconds, 0, pairs_host, geom)
+        line["gpu_vs_cpu_baseline"] = {"mixed": value / rate, "fp64": nq / (ms64 * 1e-3) / rate,
+                                       "mixed_e2e": line["e2e"]["value"] / rate}
         line["cpu_baseline"] = {
             "value": rate, "unit": "quartets/s", "cores": nthreads, "kind": "port",
             "sample": f"{n} uniformly random surviving unique shell quartets of the workload "
