@@ -41,7 +41,8 @@ extern "C" {
  *     F_m(T_k) at [k*HI_NCOL + m], m < HI_NCOL-1, k < SQ_BOYS_HI_NGRID; column
  *     HI_NCOL-1 = exp(-T_k).  Same step; tabulated to SQ_BOYS_HI_TMAX.
  * FP32 table (SQ_BOYS_TAB32_SIZE floats): the same F grid, then
- *   [SQ_BOYS_TAY32_OFF + (m*NGRID + k)*4 + j], j < 4. */
+ *   [SQ_BOYS_TAY32_OFF + (m*NGRID + k)*4 + j], j < 4, and the fifth
+ *   coefficient (j = 4) at [SQ_BOYS_TAY32_5_OFF + m*NGRID + k]. */
 #define SQ_BOYS_NGRID 580
 #define SQ_BOYS_STEP_INV 16
 #define SQ_BOYS_NCOL 16
@@ -53,7 +54,8 @@ extern "C" {
 #define SQ_BOYS_HI64_OFF (SQ_BOYS_TAY64_OFF + 16 * SQ_BOYS_NGRID * 8)
 #define SQ_BOYS_TAB64_SIZE (SQ_BOYS_HI64_OFF + SQ_BOYS_HI_NGRID * SQ_BOYS_HI_NCOL)
 #define SQ_BOYS_TAY32_OFF (SQ_BOYS_NGRID * SQ_BOYS_NCOL)
-#define SQ_BOYS_TAB32_SIZE (SQ_BOYS_TAY32_OFF + 16 * SQ_BOYS_NGRID * 4)
+#define SQ_BOYS_TAY32_5_OFF (SQ_BOYS_TAY32_OFF + 16 * SQ_BOYS_NGRID * 4)
+#define SQ_BOYS_TAB32_SIZE (SQ_BOYS_TAY32_5_OFF + 16 * SQ_BOYS_NGRID)
 
 /* Precision of one ERI / J-K launch. */
 #define SQ_FP64 0             /* all arithmetic in FP64 */

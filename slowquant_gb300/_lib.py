@@ -30,7 +30,8 @@ SQ_BOYS_HI_NCOL = 24
 SQ_BOYS_HI_TMAX = 60.0
 SQ_BOYS_HI64_OFF = SQ_BOYS_NGRID * SQ_BOYS_NCOL + 16 * SQ_BOYS_NGRID * 8
 SQ_BOYS_TAB64_SIZE = SQ_BOYS_HI64_OFF + SQ_BOYS_HI_NGRID * SQ_BOYS_HI_NCOL
-SQ_BOYS_TAB32_SIZE = SQ_BOYS_NGRID * SQ_BOYS_NCOL + 16 * SQ_BOYS_NGRID * 4
+SQ_BOYS_TAY32_5_OFF = SQ_BOYS_NGRID * SQ_BOYS_NCOL + 16 * SQ_BOYS_NGRID * 4
+SQ_BOYS_TAB32_SIZE = SQ_BOYS_TAY32_5_OFF + 16 * SQ_BOYS_NGRID
 SQ_FP64 = 0
 SQ_FP32 = 1
 SQ_FP32_BOYS32 = 2

@@ -7,7 +7,8 @@
 //     ((2m+1)(2m+3)...(2m+2i+1)) with compensated summation, and the scaled
 //     Taylor coefficients F_{m+j}(T_k)/j!, exp(-T_k)/j!;
 //   * for T < 36, F_m(T) = sum_j [F_{m+j}(T_k)/j!] (-d)^j, d = T - T_k,
-//     |d| <= 1/32 (7 terms in FP64: truncation < 6e-15 relative; 4 in FP32),
+//     |d| <= 1/32 (7 terms in FP64: truncation < 6e-15 relative; 5 in FP32:
+//     < 3e-10, so the always-positive remainder adds no FP32-sized bias),
 //     a Horner chain of FMAs only;
 //     for m_max >= 2 only F_{m_max} is expanded and the lower orders follow
 //     from the stable downward recursion (2m+1) F_m = 2T F_{m+1} + e^{-T},
@@ -27,7 +28,7 @@
 namespace sq {
 
 constexpr int kBoysTaylor64 = 7;
-constexpr int kBoysTaylor32 = 4;
+constexpr int kBoysTaylor32 = 5;
 constexpr double kSqrtPiHalf = 0.88622692545275801365;  // sqrt(pi)/2
 
 // Grid point of T (T >= 0, T < 36) computed on the FP32 / integer pipes, and
@@ -53,10 +54,6 @@ __device__ __forceinline__ double taylor7(const double *__restrict__ row, double
     return fma(f, x, c01.x);
 }
 
-__device__ __forceinline__ float taylor4(const float *__restrict__ row, float x) {
-    const float4 c = __ldg(reinterpret_cast<const float4 *>(row));
-    return fmaf(fmaf(fmaf(c.w, x, c.z), x, c.y), x, c.x);
-}
 
 // FP64: F[0..M] at T >= 0.  tab: the FP64 table (SQ_BOYS_TAB64_SIZE doubles).
 template <int M>
@@ -88,23 +85,36 @@ __device__ __forceinline__ void boys64(double T, const double *__restrict__ tab,
     }
 }
 
-// FP32 Boys from two blocks of the FP32 Taylor table (rows of 4 floats per
-// grid point; global or shared memory): for M <= 1, b0/b1 are the blocks of
-// orders 0 and 1; for M >= 2, b0 is the block of order M and b1 the exp block.
-// 4-term Taylor, truncation < 4e-8 relative.
+// The two blocks of the FP32 Taylor table an order-M evaluation reads (in
+// shared memory): coefficients 0-3 of each grid row as a float4, and the
+// fifth coefficient.  For M <= 1 the blocks are those of orders 0 and 1; for
+// M >= 2, block 0 is order M and block 1 the exp block.
+struct Boys32Blocks {
+    const float4 *c0, *c1;
+    const float *e0, *e1;
+};
+
+// 5-term Taylor sum at md = -(T - T_k).  Five terms, not four: the remainder
+// of a truncated expansion of F_m is F_{m+n}(xi) d^n / n! > 0 whatever the
+// sign of d (every derivative of order n of F_m is (-1)^n F_{m+n}), so a
+// 4-term sum is biased low by up to 4e-8 relative at |d| <= 1/32 -- a
+// coherent bias that the energy accumulates over millions of FP32 primitive
+// quartets; the fifth term brings it to 2.5e-10.
+__device__ __forceinline__ float taylor5(float4 c, float e, float md) {
+    return fmaf(fmaf(fmaf(fmaf(e, md, c.w), md, c.z), md, c.y), md, c.x);
+}
+
+// FP32 Boys from the table blocks tb; truncation < 3e-10 relative for T < 36.
 template <int M>
-__device__ __forceinline__ void boys32(float T, const float4 *b0, const float4 *b1, float (&F)[M + 1]) {
+__device__ __forceinline__ void boys32(float T, const Boys32Blocks &tb, float (&F)[M + 1]) {
     if (T < (float)SQ_BOYS_TMAX) {
         const int k = __float2int_rn(T * (float)SQ_BOYS_STEP_INV);
         const float md = k * (1.0f / SQ_BOYS_STEP_INV) - T;
-        const float4 c0 = b0[k];
-        F[M <= 1 ? 0 : M] = fmaf(fmaf(fmaf(c0.w, md, c0.z), md, c0.y), md, c0.x);
+        F[M <= 1 ? 0 : M] = taylor5(tb.c0[k], tb.e0[k], md);
         if constexpr (M == 1) {
-            const float4 c1 = b1[k];
-            F[1] = fmaf(fmaf(fmaf(c1.w, md, c1.z), md, c1.y), md, c1.x);
+            F[1] = taylor5(tb.c1[k], tb.e1[k], md);
         } else if constexpr (M >= 2) {
-            const float4 ce = b1[k];
-            const float e = fmaf(fmaf(fmaf(ce.w, md, ce.z), md, ce.y), md, ce.x);
+            const float e = taylor5(tb.c1[k], tb.e1[k], md);
             const float T2 = T + T;
 #pragma unroll
             for (int m = M - 1; m >= 0; --m) F[m] = fmaf(T2, F[m + 1], e) * (1.0f / (2 * m + 1));
@@ -125,16 +135,15 @@ __device__ __forceinline__ void boys32(float T, const float4 *b0, const float4 *
 // the results are handed back as FP32.  M <= 1 needs no recursion (each order
 // has its own FP32 expansion), so those classes stay entirely in FP32.
 template <int M>
-__device__ __forceinline__ void boys_mixed(float T, const float4 *b0, const float4 *b1, float (&F)[M + 1]) {
+__device__ __forceinline__ void boys_mixed(float T, const Boys32Blocks &tb, float (&F)[M + 1]) {
     if constexpr (M <= 1) {
-        boys32<M>(T, b0, b1, F);
+        boys32<M>(T, tb, F);
     } else {
         if (T < (float)SQ_BOYS_TMAX) {
             const int k = __float2int_rn(T * (float)SQ_BOYS_STEP_INV);
             const float md = k * (1.0f / SQ_BOYS_STEP_INV) - T;
-            const float4 c0 = b0[k], ce = b1[k];
-            const float f = fmaf(fmaf(fmaf(c0.w, md, c0.z), md, c0.y), md, c0.x);
-            const float e = fmaf(fmaf(fmaf(ce.w, md, ce.z), md, ce.y), md, ce.x);
+            const float f = taylor5(tb.c0[k], tb.e0[k], md);
+            const float e = taylor5(tb.c1[k], tb.e1[k], md);
             F[M] = f;
             const double T2 = f2d_bits(T + T), ed = f2d_bits(e);
             double fd = f2d_bits(f);
@@ -144,7 +153,7 @@ __device__ __forceinline__ void boys_mixed(float T, const float4 *b0, const floa
                 F[m] = d2f_bits(fd);
             }
         } else {
-            boys32<M>(T, b0, b1, F);
+            boys32<M>(T, tb, F);
         }
     }
 }

@@ -199,7 +199,7 @@ __device__ __forceinline__ PrimPair<R> load_prim(const sq_slots &sl, long long i
 //   W[tuv][cd] += sum_k U_k / sqrt(p+q) sum_{tau nu phi} (-1)^{tau+nu+phi} E^{cd}_{tau nu phi}(k) R_{t+tau,u+nu,v+phi}
 template <int LA, int LB, int LC, int LD, typename R, int BOYS>
 __device__ __forceinline__ void ket_loop(const EriArgs &args, R p, R Px, R Py, R Pz, const SlotDesc &kd, int k0, int k1,
-                                         const float4 *tb0, const float4 *tb1,
+                                         const Boys32Blocks &tb,
                                          R (&W)[LA + LB + 1][LA + LB + 1][LA + LB + 1][ncart(LC) * ncart(LD)]) {
     constexpr int NC = ncart(LC), ND = ncart(LD);
     constexpr int LAB = LA + LB, LCD = LC + LD, L = LAB + LCD;
@@ -222,9 +222,9 @@ __device__ __forceinline__ void ket_loop(const EriArgs &args, R p, R Px, R Py, R
         if constexpr (std::is_same<R, double>::value) {
             boys64<L>(T, args.tab64, F);
         } else if constexpr (BOYS == BOYS_FP64) {
-            boys_mixed<L>(T, tb0, tb1, F);
+            boys_mixed<L>(T, tb, F);
         } else {
-            boys32<L>(T, tb0, tb1, F);
+            boys32<L>(T, tb, F);
         }
         R fac = Uk * r;
         if constexpr (L == 0) {
@@ -379,7 +379,7 @@ __device__ __forceinline__ void bra_transform_f32_into_f64(
 // as in SQ_FP32 launches) and its FP32 block is added into the FP64 one.
 template <int LA, int LB, int LC, int LD, typename R, int BOYS, bool SPLIT>
 __device__ __forceinline__ void quartet_block(const EriArgs &args, const SlotDesc &bd, const SlotDesc &kd,
-                                              const float4 *tb0, const float4 *tb1,
+                                              const Boys32Blocks &tb,
                                               R (&acc)[ncart(LA) * ncart(LB)][ncart(LC) * ncart(LD)]) {
     static_assert(!SPLIT || std::is_same<R, double>::value, "primitive-level precision splits FP64 launches");
     constexpr int NAB = ncart(LA) * ncart(LB), NCD = ncart(LC) * ncart(LD);
@@ -406,7 +406,7 @@ __device__ __forceinline__ void quartet_block(const EriArgs &args, const SlotDes
         if (!SPLIT || K > 0) {
             R W[LAB + 1][LAB + 1][LAB + 1][NCD];
             zero_w<LA, LB, LC, LD, R>(W);
-            ket_loop<LA, LB, LC, LD, R, BOYS>(args, br.p, br.x, br.y, br.z, kd, 0, SPLIT ? K : nk, tb0, tb1, W);
+            ket_loop<LA, LB, LC, LD, R, BOYS>(args, br.p, br.x, br.y, br.z, kd, 0, SPLIT ? K : nk, tb, W);
             bra_transform<LA, LB, LC, LD, R>(hb + (long long)i * EB * sb, sb, R(kTwoPi52) * br.u, W, acc);
         }
         if constexpr (SPLIT) {
@@ -415,7 +415,7 @@ __device__ __forceinline__ void quartet_block(const EriArgs &args, const SlotDes
                 const float ub = (float)kTwoPi52 * __ldg(sl.prim32v + 8 * ib + 4);
                 float W32[LAB + 1][LAB + 1][LAB + 1][NCD];
                 zero_w<LA, LB, LC, LD, float>(W32);
-                ket_loop<LA, LB, LC, LD, float, BOYS_FP64>(args, b4.x, b4.y, b4.z, b4.w, kd, K, nk, tb0, tb1, W32);
+                ket_loop<LA, LB, LC, LD, float, BOYS_FP64>(args, b4.x, b4.y, b4.z, b4.w, kd, K, nk, tb, W32);
                 bra_transform_f32_into_f64<LA, LB, LC, LD>(sl.herm32 + bd.hbase + (long long)i * EB * sb, sb, ub,
                                                            W32, acc);
             }
@@ -602,17 +602,20 @@ __global__ void __launch_bounds__(128, kMinBlocks(LA + LB + LC + LD)) eri_class_
     // wavefront per 8 lanes instead of one L1 sector per lane).
     constexpr bool TAB32 = std::is_same<R, float>::value || SPLIT;
     __shared__ float4 s_tab[TAB32 ? 2 : 1][TAB32 ? SQ_BOYS_NGRID : 1];
-    const float4 *tb0 = nullptr, *tb1 = nullptr;
+    __shared__ float s_tab5[TAB32 ? 2 : 1][TAB32 ? SQ_BOYS_NGRID : 1];
+    Boys32Blocks tb{nullptr, nullptr, nullptr, nullptr};
     if constexpr (TAB32) {
         const float4 *g = reinterpret_cast<const float4 *>(args.tab32 + SQ_BOYS_TAY32_OFF);
+        const float *g5 = args.tab32 + SQ_BOYS_TAY32_5_OFF;
         const int blk0 = boys32_block<L>(0), blk1 = boys32_block<L>(1);
         for (int x = threadIdx.x; x < SQ_BOYS_NGRID; x += blockDim.x) {
             s_tab[0][x] = g[blk0 * SQ_BOYS_NGRID + x];
             s_tab[1][x] = g[blk1 * SQ_BOYS_NGRID + x];
+            s_tab5[0][x] = g5[blk0 * SQ_BOYS_NGRID + x];
+            s_tab5[1][x] = g5[blk1 * SQ_BOYS_NGRID + x];
         }
         __syncthreads();
-        tb0 = s_tab[0];
-        tb1 = s_tab[1];
+        tb = Boys32Blocks{s_tab[0], s_tab[1], s_tab5[0], s_tab5[1]};
     }
     const int nd = args.nd > 1 ? args.nd : 1;
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -633,7 +636,7 @@ __global__ void __launch_bounds__(128, kMinBlocks(LA + LB + LC + LD)) eri_class_
         }
 
         R acc[NAB][NCD];
-        quartet_block<LA, LB, LC, LD, R, BOYS, SPLIT>(args, bd, kd, tb0, tb1, acc);
+        quartet_block<LA, LB, LC, LD, R, BOYS, SPLIT>(args, bd, kd, tb, acc);
         if constexpr (!PREFETCH_D) {
             load_desc_epilogue(args.slots.desc, pq.x, bd);
             load_desc_epilogue(args.slots.desc, pq.y, kd);

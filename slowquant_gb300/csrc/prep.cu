@@ -53,6 +53,7 @@ __global__ void boys_taylor_kernel(double *tab64, float *tab32) {
     }
     tab64[SQ_BOYS_TAY64_OFF + idx] = val;
     if (tab32 && j < 4) tab32[SQ_BOYS_TAY32_OFF + mk * 4 + j] = (float)val;
+    if (tab32 && j == 4) tab32[SQ_BOYS_TAY32_5_OFF + mk] = (float)val;
 }
 
 __global__ void boys_eval_kernel(int n_max, const double *z, long long nz, const double *tab, int mode,
