@@ -460,6 +460,23 @@ def gpu_arm(args) -> None:
                            "fp32_list_quartets": p32.nquartet,
                            "mixed_builds": sum(1 for b in jkp.builds if b != "fp64"), "builds": len(jkp.builds)})
 
+    # launch shapes from the project's autotuner on this workload's lists, timed beside the defaults
+    tuned = None
+    if args.autotune:
+        from slowquant_gb300 import autotune
+
+        def run_class(sub, prec):
+            eng.jk_accumulate(D, [sub], [prec], prim_tau=FP32_THR)
+
+        t0 = time.time()
+        table = autotune.tune(run_class, [q64, q32], ["fp64", "fp32"])
+        tune_s = time.time() - t0
+        ms_tuned = float(np.median(time_events(torch, step_mixed, 5, flush)))
+        ms64_tuned = float(np.median(time_events(torch, step_fp64, 3, flush)))
+        autotune.reset()
+        tuned = {"mixed_ms": ms_tuned, "fp64_ms": ms64_tuned, "tune_s": round(tune_s, 1),
+                 "shapes": {f"{c}:{p}": [t, b] for (c, p), (t, b, _) in sorted(table.items()) if t}}
+
     # the two halves of the mixed build, each timed alone (all its classes, stream pool)
     ms_part = {}
     for name, lst, prec in (("fp64_list", q64, "fp64"), ("fp32_list", q32, "fp32")):
@@ -550,6 +567,7 @@ def gpu_arm(args) -> None:
         "tau_sweep": sweep,
         "chunk_precision": chunk_modes,
         "prim_precision": prim_modes,
+        "autotuned_launch_shapes": tuned,
         "kernels_by_time": rows[:8],
         "fp32_kernels_by_time": [r for r in rows if r["precision"] == "fp32"][:8],
         "gpu_launches": launches * args.steps,
@@ -733,6 +751,8 @@ def main() -> None:
     ap.add_argument("--jk-streams", type=int, default=0, help="J/K class launch streams (0: library default)")
     ap.add_argument("--tau-sweep", type=float, nargs="*", default=[1e-5, 1e-4, 1e-3, 1e-2, 1e-1],
                     help="FP32 Schwarz thresholds reported beside the headline (empty: skip)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="also time the build with the autotuner's launch shapes for this workload")
     ap.add_argument("--prim-sweep", type=float, nargs="*", default=[1e-4, 1e-3, 1e-2],
                     help="bounds of the primitive-level precision mode reported beside the headline (empty: skip)")
     args = ap.parse_args()

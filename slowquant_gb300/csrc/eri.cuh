@@ -85,10 +85,24 @@ __device__ __forceinline__ const R *slot_herm_ptr(const sq_slots &sl) {
         return sl.herm32;
 }
 
+// x^{-1/2} in FP64 with few FP64 instructions (the FP64 pipe bounds these
+// kernels; the FP32 and integer pipes are idle): an FP32 estimate y0 (about 23
+// correct bits, conversions on the integer pipe) refined by one step of
+// Newton's iteration for f(y) = y^{-2} - x carried to second order,
+//   e = 1 - x y0^2,   y = y0 (1 + e/2 + 3 e^2 / 8),
+// whose error is O(e^3), below the FP64 rounding for |e| < 1e-6.  Five FP64
+// operations.  x must be a positive normal double in the FP32 range.
+__device__ __forceinline__ double rsqrt_f64(double x) {
+    const double y0 = f2d_bits(rsqrtf(d2f_bits(x)));
+    const double e = fma(-x * y0, y0, 1.0);
+    const double y0e = y0 * e;
+    return fma(y0e, fma(0.375, e, 0.5), y0);
+}
+
 template <typename R>
 __device__ __forceinline__ R rsqrt_r(R x) {
     if constexpr (std::is_same<R, double>::value)
-        return rsqrt(x);
+        return rsqrt_f64(x);
     else
         return rsqrtf(x);
 }
