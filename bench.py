@@ -534,6 +534,20 @@ def gpu_arm(args) -> None:
         small.append({"system": "H2O", "basis": basis, "eri_tensor_s": float(np.median(te)),
                       "scf_s": float(np.median(ts)), "E_hf": A.hartree_fock.E_hf})
 
+    # AO -> MO transform (integralfunctions.py:199-211) on an n = m = 128 tensor: the four
+    # rotate passes of sq_ao2mo_rotate, 2 n^4 m + 2 n^3 m^2 + 2 n^2 m^3 + 2 n m^4 FLOPs
+    from slowquant_gb300.integralfunctions import two_electron_integral_transform
+
+    na = 128
+    gA = torch.randn((na, na, na, na), dtype=torch.float64, device="cuda")
+    cA = torch.randn((na, na), dtype=torch.float64, device="cuda")
+    two_electron_integral_transform(cA, gA)
+    ms_ao2mo = float(np.median(time_events(torch, lambda: two_electron_integral_transform(cA, gA), 5, flush)))
+    fl_ao2mo = 8.0 * na ** 5
+    ao2mo = {"n": na, "m": na, "ms": ms_ao2mo, "tflops": fl_ao2mo / (ms_ao2mo * 1e-3) / 1e12,
+             "frac_of_fp64_fma_peak": fl_ao2mo / (ms_ao2mo * 1e-3) / peak64}
+    del gA
+
     clocks = clk.summary()
     line = {
         "metric": METRIC, "value": value, "unit": "quartets/s", "n_gpus": world, "steps": args.steps,
@@ -564,6 +578,7 @@ def gpu_arm(args) -> None:
         "roofline_fp64_build": {"flops": fl64, "ms": ms64, "achieved_tflops": fl64 / (ms64 * 1e-3) / 1e12,
                                 "peak_tflops": peak64 / 1e12, "frac": fl64 / (ms64 * 1e-3) / peak64},
         "small_systems": small,
+        "ao2mo": ao2mo,
         "tau_sweep": sweep,
         "chunk_precision": chunk_modes,
         "prim_precision": prim_modes,

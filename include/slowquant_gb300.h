@@ -353,6 +353,15 @@ int sq_grad_2e(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slo
 int sq_grad_1e(const sq_basis *basis, const double *table64, const double *D, const double *W, double *grad,
                void *stream);
 
+/* One pass of the AO -> MO transformation (slowquant/molecularintegrals/
+ * integralfunctions.py:186-211, which contracts with numpy einsum):
+ *   out[l][r] = sum_{d < n} G[r][d] C[d][l],   r < rows, l < m,
+ * G rows x n and C n x m row-major, out m x rows.  Transforming the last index
+ * and moving it to the front, four passes turn g[a][b][c][d] into
+ * g[i][j][k][l] (rows = n^3, m n^2, m^2 n, m^3) and two turn h into C^T h C.
+ * out must not alias G.  FP64 arithmetic. */
+int sq_ao2mo_rotate(long long rows, int n, int m, const double *G, const double *C, double *out, void *stream);
+
 /* Batched symmetric eigensolver (replaces the per-molecule numpy eigh of the
  * SCF step, slowquant/hartreefock/hartreefock_in_memory.py:63-66, when many
  * molecules run at once).  Matrix i is dims[i] x dims[i] (1..128), row-major

@@ -158,6 +158,25 @@ def test_ao_to_mo_transforms_match_einsum(gpu_lib, golden_energies):
                                np.einsum("ai,bj,ck,dl,abcd->ijkl", Ca, Ca, Ca, Ca, g, optimize=True), atol=1e-11)
 
 
+def test_ao_to_mo_rotate_kernel_ragged_sizes(gpu_lib):
+    """sq_ao2mo_rotate at sizes that are not multiples of its 64 x 64 x 16 tiles, against numpy."""
+    import torch
+
+    from slowquant_gb300.integralfunctions import one_electron_integral_transform, two_electron_integral_transform
+
+    rng = np.random.default_rng(4)
+    for n, m in ((37, 23), (17, 17), (65, 3), (5, 70)):
+        C = rng.standard_normal((n, m))
+        g = rng.standard_normal((n, n, n, n)) if n <= 40 else None
+        h = rng.standard_normal((n, n))
+        np.testing.assert_allclose(one_electron_integral_transform(C, h), C.T @ h @ C, atol=1e-11)
+        if g is not None:
+            ref = np.einsum("ai,bj,ck,dl,abcd->ijkl", C, C, C, C, g, optimize=True)
+            out = two_electron_integral_transform(torch.tensor(C, device="cuda"), torch.tensor(g, device="cuda"))
+            assert isinstance(out, torch.Tensor)
+            np.testing.assert_allclose(out.cpu().numpy(), ref, atol=1e-9 * np.abs(ref).max())
+
+
 H6_BOHR = ";".join(f"H   {float(i):.12f}   0.000000000000   0.000000000000" for i in range(6))
 
 
