@@ -328,6 +328,13 @@ int sq_fock_build(int nbf, const double *H, const double *Jacc, const double *Ka
 int sq_one_electron(const sq_basis *basis, const double *table64, double *S, double *T, double *V,
                     void *stream);
 
+/* Multipole integral matrix M[nbf][nbf] = <a| (x-Cx)^ex (y-Cy)^ey (z-Cz)^ez |b>
+ * (multipole_integral_driver, slowquant/molecularintegrals/multipole.py:10-135,
+ * with the Hermite multipole recursion of integralfunctions.py:151-183).
+ * order (host, [3]) = (ex, ey, ez), each 0..16; origin (host, [3]) = C in the
+ * coordinates of basis->center.  order (0,0,0) is the overlap. */
+int sq_multipole(const sq_basis *basis, const int *order, const double *origin, double *M, void *stream);
+
 /* Expand per-bra tasks into the flat quartet list: task i writes
  * (bra[i], ket_list[ket_start[i] + k]) for k < count[i] at out[offset[i] + k],
  * or (bra[i], ket_start[i] + k) when ket_list is NULL (slot ids).  offset is

@@ -327,6 +327,87 @@ __global__ void one_electron_kernel(const sq_basis basis, const double *tab, dou
         }
 }
 
+// Multipole integrals <a| (x-Cx)^ex (y-Cy)^ey (z-Cz)^ez |b> over contracted
+// Cartesian shells (slowquant/molecularintegrals/multipole.py:48-135): per
+// primitive pair and dimension, the Hermite multipole integrals of
+// integralfunctions.py:151-183,
+//   M^0_0 = sqrt(pi/p),  M^{e+1}_t = t M^e_{t-1} + X_PC M^e_t + M^e_{t+1} / (2p),
+// contracted with the expansion coefficients: S = prod_d sum_{t <= min(a_d+b_d, e_d)} E^{ab}_t M^{e_d}_t.
+// One shell pair per thread, both triangles written (the matrix is symmetric).
+constexpr int kMultipoleMax = 16;  // highest order per Cartesian direction
+
+__global__ void multipole_kernel(const sq_basis basis, int ex, int ey, int ez, double cx, double cy, double cz,
+                                 double *M) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ns = basis.nshell;
+    if (idx >= ns * (ns + 1) / 2) return;
+    int s1 = (int)((sqrt(8.0 * idx + 1.0) - 1.0) * 0.5);
+    while ((s1 + 1) * (s1 + 2) / 2 <= idx) ++s1;
+    while (s1 * (s1 + 1) / 2 > idx) --s1;
+    const int s2 = idx - s1 * (s1 + 1) / 2;
+    if (basis.mat_base != nullptr && basis.mat_base[s1] != basis.mat_base[s2]) return;
+    const int l1 = basis.l[s1], l2 = basis.l[s2];
+    const int n1 = ncart(l1), n2 = ncart(l2);
+    const int np1 = basis.nprim[s1], np2 = basis.nprim[s2];
+    const double *A = basis.center + 3 * s1, *B = basis.center + 3 * s2;
+    const double C[3] = {cx, cy, cz};
+    const int eo[3] = {ex, ey, ez};
+    double blk[100];
+    for (int x = 0; x < n1 * n2; ++x) blk[x] = 0.0;
+    double E[3][kE1][kE1][2 * kE1 - 1];
+    double Mh[3][kMultipoleMax + 1];  // M^{e_d}_t, t <= e_d, of each direction
+    double row[kMultipoleMax + 1], nxt[kMultipoleMax + 1];
+    constexpr double pi = 3.141592653589793;
+    for (int i = 0; i < np1; ++i)
+        for (int j = 0; j < np2; ++j) {
+            const double al = basis.exps[basis.prim_off[s1] + i], be = basis.exps[basis.prim_off[s2] + j];
+            const double cc = basis.coefs[basis.prim_off[s1] + i] * basis.coefs[basis.prim_off[s2] + j];
+            const double p = al + be, mu = al * be / p;
+            double Pc[3], AB2 = 0.0;
+            for (int d = 0; d < 3; ++d) {
+                Pc[d] = (al * A[d] + be * B[d]) / p;
+                AB2 += (A[d] - B[d]) * (A[d] - B[d]);
+            }
+            const double K = exp(-mu * AB2);
+            for (int d = 0; d < 3; ++d) {
+                ecoef_1d_big(Pc[d] - A[d], Pc[d] - B[d], 0.5 / p, l1, l2, E[d]);
+                const double X = Pc[d] - C[d];
+                for (int t = 0; t <= eo[d]; ++t) row[t] = 0.0;
+                row[0] = sqrt(pi / p);
+                for (int e = 0; e < eo[d]; ++e) {  // row holds M^e_t; build M^{e+1}_t
+                    for (int t = 0; t <= e + 1; ++t) {
+                        double v = X * (t <= e ? row[t] : 0.0);
+                        if (t > 0) v += t * row[t - 1];
+                        if (t + 1 <= e) v += (0.5 / p) * row[t + 1];
+                        nxt[t] = v;
+                    }
+                    for (int t = 0; t <= e + 1; ++t) row[t] = nxt[t];
+                }
+                for (int t = 0; t <= eo[d]; ++t) Mh[d][t] = row[t];
+            }
+            for (int x = 0; x < n1; ++x) {
+                const int a[3] = {cart_x(l1, x), cart_y(l1, x), cart_z(l1, x)};
+                const double na = comp_norm(l1, x);
+                for (int y = 0; y < n2; ++y) {
+                    const int b[3] = {cart_x(l2, y), cart_y(l2, y), cart_z(l2, y)};
+                    double prod = cc * K * na * comp_norm(l2, y);
+                    for (int d = 0; d < 3; ++d) {
+                        const int tmax = a[d] + b[d] < eo[d] ? a[d] + b[d] : eo[d];
+                        double sdim = 0.0;
+                        for (int t = 0; t <= tmax; ++t) sdim += E[d][a[d]][b[d]][t] * Mh[d][t];
+                        prod *= sdim;
+                    }
+                    blk[x * n2 + y] += prod;
+                }
+            }
+        }
+    for (int x = 0; x < n1; ++x)
+        for (int y = 0; y < n2; ++y) {
+            const long long rc = mat_index(basis, s1, x, s2, y), cr = mat_index(basis, s2, y, s1, x);
+            M[rc] = M[cr] = blk[x * n2 + y];
+        }
+}
+
 // ---------------------------------------------------------------------------
 __global__ void quartets_expand_kernel(long long ntask, const int *bra, const int *ket_start, const int *count,
                                        const long long *offset, const int *ket_list, int2 *out, long long nout) {
@@ -460,6 +541,19 @@ extern "C" int sq_one_electron(const sq_basis *basis, const double *table64, dou
     if (np == 0) return SQ_OK;
     one_electron_kernel<<<(np + 63) / 64, 64, 0, (cudaStream_t)stream>>>(*basis, table64, S, T, V);
     return check_launch("sq_one_electron");
+}
+
+extern "C" int sq_multipole(const sq_basis *basis, const int *order, const double *origin, double *M,
+                            void *stream) {
+    if (!basis || !order || !origin || !M) return set_error(SQ_ERR_ARG, "sq_multipole: NULL argument");
+    for (int d = 0; d < 3; ++d)
+        if (order[d] < 0 || order[d] > kMultipoleMax)
+            return set_error(SQ_ERR_ARG, "sq_multipole: order %d out of range 0..%d", order[d], kMultipoleMax);
+    const int np = basis->nshell * (basis->nshell + 1) / 2;
+    if (np == 0) return SQ_OK;
+    multipole_kernel<<<(np + 63) / 64, 64, 0, (cudaStream_t)stream>>>(*basis, order[0], order[1], order[2],
+                                                                       origin[0], origin[1], origin[2], M);
+    return check_launch("sq_multipole");
 }
 
 extern "C" int sq_quartets_expand(long long ntask, const int *bra, const int *ket_start, const int *count,

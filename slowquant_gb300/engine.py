@@ -678,6 +678,20 @@ class IntegralEngine:
                                        self._stream()), "sq_one_electron")
         return S, T, V
 
+    def multipole(self, order, origin=None) -> torch.Tensor:
+        """Multipole matrix <a| (x-Cx)^ex (y-Cy)^ey (z-Cz)^ez |b> (nbf x nbf FP64 device tensor).
+
+        origin: C in bohr, in the molecule's own coordinates (default: its
+        centre of mass, as multipole.py:10-45 uses)."""
+        n = self.nbf
+        o = np.asarray(order, dtype=np.int32).reshape(3)
+        c = (self.mol.center_of_mass if origin is None else np.asarray(origin, dtype=np.float64)) - self.origin
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        M = torch.zeros((n, n), dtype=torch.float64, device=self.device)
+        check(self.lib.sq_multipole(ctypes.byref(self.cbasis), o.ctypes.data, c.ctypes.data, ptr(M), self._stream()),
+              "sq_multipole")
+        return M
+
     def eri_dense(self, threshold: float = 1e-12) -> torch.Tensor:
         """Dense (nbf,)*4 FP64 ERI tensor on the device, screened like the reference driver."""
         return self.eri_dense_with_q(self.pair_q, threshold)

@@ -130,7 +130,10 @@ class _Integral:
         return self._eri()
 
     def get_multipole_matrix(self, multipole_order) -> np.ndarray:
-        """Only the zeroth moment (the overlap) is provided on this path."""
-        if np.any(np.asarray(multipole_order) != 0):
-            raise NotImplementedError("multipole integrals beyond the overlap are outside this package")
-        return self.overlap_matrix.copy()
+        """Multipole integrals of Cartesian orders (ex, ey, ez) about the centre of mass
+        (integralclass.py:99-108, multipole.py:10-135); (0, 0, 0) is the overlap."""
+        M = self.engine.multipole(np.asarray(multipole_order, dtype=np.int64))
+        if self.spherical:
+            Tm = self.cart_to_sph
+            M = Tm.T @ M @ Tm
+        return M.cpu().numpy()

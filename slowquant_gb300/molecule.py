@@ -33,12 +33,22 @@ _SYMBOLS = (
     "Lu Hf Ta W Re Os Ir Pt Au Hg Tl Pb Bi Po At Rn"
 ).split()
 CHARGE = {s: i + 1 for i, s in enumerate(_SYMBOLS)}
-# Standard atomic weights (IUPAC, abridged), used only for the centre of mass.
-MASS = dict(zip(_SYMBOLS[:36], [
-    1.008, 4.0026, 6.94, 9.0122, 10.81, 12.011, 14.007, 15.999, 18.998, 20.180, 22.990, 24.305, 26.982,
-    28.085, 30.974, 32.06, 35.45, 39.948, 39.098, 40.078, 44.956, 47.867, 50.942, 51.996, 54.938, 55.845,
-    58.933, 58.693, 63.546, 65.38, 69.723, 72.630, 74.922, 78.971, 79.904, 83.798,
-]))
+# Standard atomic weights as the reference tabulates them (slowquant/molecule/constants.py),
+# used for the centre of mass (the origin of the multipole integrals).  Elements the
+# reference gives no weight (Tc, Pm, Po, At, Rn) weigh 0 in the centre of mass, as there.
+MASS = {
+    "H": 1.008, "He": 4.002, "Li": 6.94, "Be": 9.012, "B": 10.81, "C": 12.011, "N": 14.007, "O": 15.999, "F":
+    18.998, "Ne": 20.1797, "Na": 22.989, "Mg": 24.305, "Al": 26.981, "Si": 28.085, "P": 30.973, "S": 32.06,
+    "Cl": 35.45, "Ar": 39.948, "K": 39.0983, "Ca": 40.078, "Sc": 44.955, "Ti": 47.867, "V": 50.9415, "Cr":
+    51.9961, "Mn": 54.938, "Fe": 55.845, "Co": 58.933, "Ni": 58.6934, "Cu": 63.546, "Zn": 65.38, "Ga": 69.723,
+    "Ge": 72.63, "As": 74.921, "Se": 78.971, "Br": 79.904, "Kr": 83.798, "Rb": 85.4678, "Sr": 87.62, "Y":
+    88.905, "Zr": 91.224, "Nb": 92.906, "Mo": 95.95, "Ru": 101.07, "Rh": 102.905, "Pd": 106.42, "Ag": 107.8682,
+    "Cd": 112.414, "In": 114.818, "Sn": 118.71, "Sb": 121.76, "Te": 127.6, "I": 126.904, "Xe": 131.293, "Cs":
+    132.905, "Ba": 137.327, "La": 138.905, "Ce": 140.116, "Pr": 140.907, "Nd": 144.242, "Sm": 150.36, "Eu":
+    151.964, "Gd": 157.25, "Tb": 158.925, "Dy": 162.5, "Ho": 164.93, "Er": 167.259, "Tm": 168.934, "Yb":
+    173.045, "Lu": 174.9668, "Hf": 178.49, "Ta": 180.947, "W": 183.84, "Re": 186.207, "Os": 190.23, "Ir":
+    192.217, "Pt": 195.084, "Au": 196.966, "Hg": 200.592, "Tl": 204.38, "Pb": 207.2, "Bi": 208.98,
+}
 
 # Cartesian component order per shell (basis_reader.py:50-70).
 CARTESIAN = {
@@ -55,7 +65,7 @@ def atom_to_properties(atom_name: str, atom_property: str) -> float:
     if atom_property == "charge":
         return CHARGE[atom_name]
     if atom_property == "mass":
-        return MASS.get(atom_name, 2.0 * CHARGE[atom_name])
+        return MASS.get(atom_name, 0.0)
     raise ValueError(f"unknown atom property {atom_property}")
 
 

@@ -285,6 +285,28 @@ def main() -> None:
         np.savez_compressed(os.path.join(out, "primitives.npz"), **prim)
         print("primitives done", flush=True)
 
+    if want("multipole"):
+        # the reference's multipole matrices (about its centre of mass) for water in 6-31G* and
+        # H2O2 in cc-pVTZ (f shells): dipole, quadrupole and some higher mixed orders
+        orders = [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (2, 0, 0), (1, 1, 0), (0, 1, 1), (0, 0, 2),
+                  (3, 0, 0), (1, 2, 3)]
+        sets = {"h2o_631gs": orders, "h2o2_ccpvtz": [(1, 0, 0), (0, 1, 1), (0, 0, 2), (1, 2, 3)]}
+        res = {}
+        for tag, geom, unit, basis in (("h2o_631gs", H2O_CRAWFORD_BOHR, "bohr", "6-31G*"),
+                                       ("h2o2_ccpvtz", H2O2_ANGSTROM, "angstrom", "cc-pvtz")):
+            orders = sets[tag]
+            res[f"{tag}_orders"] = np.array(orders)
+            A = sq.SlowQuant()
+            A.set_molecule(geom, distance_unit=unit)
+            A.set_basis_set(basis)
+            res[f"{tag}_com"] = A.molecule.center_of_mass
+            res[f"{tag}_M"] = np.stack([A.integral.get_multipole_matrix(np.array(o)) for o in orders])
+            res[f"{tag}_geometry"] = np.array(geom)
+            res[f"{tag}_unit"] = np.array(unit)
+            res[f"{tag}_basis"] = np.array(basis)
+        np.savez_compressed(os.path.join(out, "multipole.npz"), **res)
+        print("multipole done", flush=True)
+
     if want("h2o2_ccpvtz_f"):
         from slowquant.molecularintegrals.electronrepulsion import electron_repulsion_integral
 

@@ -426,3 +426,11 @@ def test_dropin_aliases_resolve_and_uninstall_cleanly():
         dropin.uninstall(saved)
     after = {k: v for k, v in sys.modules.items() if k == "slowquant" or k.startswith("slowquant.")}
     assert after == before
+
+
+def test_centre_of_mass_uses_the_reference_masses():
+    """The multipole origin: the reference's centre of mass (its mass table) for the golden molecules."""
+    g = load_golden("multipole")
+    for tag in ("h2o_631gs", "h2o2_ccpvtz"):
+        m = molecule._Molecule(str(g[f"{tag}_geometry"]), 0, str(g[f"{tag}_unit"]))
+        np.testing.assert_allclose(m.center_of_mass, g[f"{tag}_com"], atol=1e-12)
