@@ -273,6 +273,13 @@ int sq_jk(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, c
           const double *table64, const float *table32, const double *D, float *D32, double *Jacc, double *Kacc,
           int precision, void *stream);
 
+/* J and K from a stored ERI tensor V[nbf^4] (C order): J[p][q] =
+ * sum_rs V[p][q][r][s] D[s][r] and K[p][q] = sum_rs V[p][s][q][r] D[s][r], the
+ * two einsums of run_hartree_fock when it is given the tensor
+ * (hartreefock_in_memory.py:55-56), in one pass over V.  J and K ([nbf][nbf])
+ * are overwritten. */
+int sq_jk_dense(int nbf, const double *V, const double *D, double *J, double *K, void *stream);
+
 /* Several densities per integral evaluation (the two spin densities of
  * unrestricted HF, slowquant/hartreefock/unrestricted_hartreefock_in_memory.py:69-74,
  * which the reference contracts four times with the stored tensor): like

@@ -137,6 +137,7 @@ def lib() -> ctypes.CDLL:
         L.sq_grad_1e.argtypes = [ctypes.POINTER(SqBasis), _p, _p, _p, _p, _p]
         L.sq_ao2mo_rotate.argtypes = [ctypes.c_longlong, ctypes.c_int, ctypes.c_int, _p, _p, _p, _p]
         L.sq_multipole.argtypes = [ctypes.POINTER(SqBasis), _p, _p, _p, _p]
+        L.sq_jk_dense.argtypes = [ctypes.c_int, _p, _p, _p, _p, _p]
         L.sq_jk_prim.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
                                  ctypes.POINTER(SqQuartets), _p, _p, _p, _p, _p, ctypes.c_double, _p]
         L.sq_jk_noalloc.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
@@ -154,7 +155,7 @@ def lib() -> ctypes.CDLL:
 EXPORTED = [
     "sq_version", "sq_last_error", "sq_set_option", "sq_get_option", "sq_set_launch_config", "sq_boys_table", "sq_boys",
     "sq_pair_prep", "sq_schwarz", "sq_eri_dense", "sq_jk", "sq_fock_build", "sq_one_electron",
-    "sq_quartets_expand", "sq_fma_probe", "sq_slots_fill", "sq_slots_describe", "sq_jk_prim", "sq_ao2mo_rotate", "sq_multipole", "sq_jk_noalloc", "sq_grad_2e", "sq_grad_1e",
+    "sq_quartets_expand", "sq_fma_probe", "sq_slots_fill", "sq_slots_describe", "sq_jk_prim", "sq_ao2mo_rotate", "sq_multipole", "sq_jk_dense", "sq_jk_noalloc", "sq_grad_2e", "sq_grad_1e",
     "sq_batched_eigh", "sq_jk_multi",
 ]
 

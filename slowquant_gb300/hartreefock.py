@@ -4,9 +4,10 @@ Drop-in for slowquant/hartreefock/{hartreefock_in_memory.py,
 unrestricted_hartreefock_in_memory.py, diis.py,
 hartreefockclass.py}: same names, arguments, iteration semantics and log lines.
 Linear algebra runs on the device in FP64 (torch: cuSOLVER eigh, cuBLAS
-products).  The two-electron part comes either from a dense ERI tensor
-(the reference's einsums, hartreefock_in_memory.py:55-56) or from the
-integral-direct J/K kernels (``DirectJK``), optionally in mixed precision.
+products).  The two-electron part comes either from a dense ERI tensor (the
+reference's einsums, hartreefock_in_memory.py:55-56, as one pass of the
+library's ``sq_jk_dense`` over the tensor) or from the integral-direct J/K
+kernels (``DirectJK``), optionally in mixed precision.
 """
 
 from __future__ import annotations
@@ -15,6 +16,22 @@ import numpy as np
 import torch
 
 from .logger import _Logger
+
+
+def dense_jk(G: torch.Tensor, D: torch.Tensor):
+    """J = einsum("pqrs,sr->pq", G, D) and K = einsum("psqr,sr->pq", G, D)
+    (hartreefock_in_memory.py:55-56) from a stored (n,)*4 tensor in one pass over it
+    (the library's sq_jk_dense)."""
+    from . import _lib
+
+    n = G.shape[0]
+    G = G.contiguous()
+    D = D.to(dtype=torch.float64).contiguous()
+    J = torch.empty((n, n), dtype=torch.float64, device=G.device)
+    K = torch.empty_like(J)
+    _lib.check(_lib.lib().sq_jk_dense(n, _lib.ptr(G), _lib.ptr(D), _lib.ptr(J), _lib.ptr(K), _lib.stream_handle()),
+               "sq_jk_dense")
+    return J, K
 
 
 def _dev_tensor(x, device) -> torch.Tensor:
@@ -140,7 +157,7 @@ def run_hartree_fock(S, T, V, ERI, number_electrons: int, log, dE_threshold: flo
         G = _dev_tensor(ERI, device)
 
         def jk(D):
-            return torch.einsum("pqrs,sr->pq", G, D), torch.einsum("psqr,sr->pq", G, D)
+            return dense_jk(G, D)
 
     Lambda_S, L_S = torch.linalg.eigh(S)
     S_sqrt = L_S @ torch.diag(Lambda_S ** (-1 / 2)) @ L_S.T
@@ -311,7 +328,7 @@ def run_unrestricted_hartree_fock(S, T, V, ERI, number_electrons_alpha: int, num
         G = _dev_tensor(ERI, device)
 
         def jk(D):
-            return torch.einsum("pqrs,sr->pq", G, D), torch.einsum("psqr,sr->pq", G, D)
+            return dense_jk(G, D)
 
     na, nb = int(number_electrons_alpha), int(number_electrons_beta)
     Lambda_S, L_S = torch.linalg.eigh(S)

@@ -158,6 +158,24 @@ def test_ao_to_mo_transforms_match_einsum(gpu_lib, golden_energies):
                                np.einsum("ai,bj,ck,dl,abcd->ijkl", Ca, Ca, Ca, Ca, g, optimize=True), atol=1e-11)
 
 
+def test_dense_jk_kernel_matches_einsum(gpu_lib):
+    """sq_jk_dense (one pass over the stored tensor) against the reference's two einsums,
+    with D in shared memory (n = 37) and read through the caches (n = 120)."""
+    import torch
+
+    from slowquant_gb300.hartreefock import dense_jk
+
+    rng = np.random.default_rng(6)
+    for n in (37, 120):
+        G = torch.tensor(rng.standard_normal((n, n, n, n)), device="cuda")
+        D = torch.tensor(rng.standard_normal((n, n)), device="cuda")
+        J, K = dense_jk(G, D)
+        Jr = torch.einsum("pqrs,sr->pq", G, D)
+        Kr = torch.einsum("psqr,sr->pq", G, D)
+        torch.testing.assert_close(J, Jr, rtol=0, atol=1e-10 * float(Jr.abs().max()))
+        torch.testing.assert_close(K, Kr, rtol=0, atol=1e-10 * float(Kr.abs().max()))
+
+
 def test_ao_to_mo_rotate_kernel_ragged_sizes(gpu_lib):
     """sq_ao2mo_rotate at sizes that are not multiples of its 64 x 64 x 16 tiles, against numpy."""
     import torch
@@ -229,3 +247,32 @@ def test_edge_cases_small_systems(gpu_lib):
     D = torch.eye(eng.nbf, dtype=torch.float64, device="cuda")
     J, K = eng.jk(D, 1e30, "mixed", 1e-4)
     assert float(J.abs().max()) == 0.0 and float(K.abs().max()) == 0.0
+
+
+def test_torch_operators_match_the_package_calls(gpu_lib):
+    """torch.ops.slowquant_gb300.* give the package functions' results on CUDA tensors."""
+    import torch
+
+    import slowquant_gb300.torch_ops as ops
+    from slowquant_gb300 import systems
+    from slowquant_gb300.engine import IntegralEngine
+    from slowquant_gb300.hartreefock import dense_jk
+    from slowquant_gb300.molecule import _Molecule
+
+    m = _Molecule(systems.water_monomer(), 0, "angstrom")
+    m._set_basis_set("6-31G*")
+    eng = IntegralEngine(m)
+    V = eng.eri_dense(1e-12)
+    rng = np.random.default_rng(8)
+    C = rng.standard_normal((eng.nbf, eng.nbf // 2))
+    D = torch.tensor(2 * C @ C.T, device="cuda")
+    Jo, Ko = torch.ops.slowquant_gb300.jk_dense(V, D)
+    Jd, Kd = dense_jk(V, D)
+    torch.testing.assert_close(Jo, Jd, rtol=0, atol=0)
+    h = ops.register_engine(eng)
+    Jx, Kx = torch.ops.slowquant_gb300.direct_jk(h, D, 1e-12, "fp64", 1e-4)
+    torch.testing.assert_close(Jx, Jd, rtol=0, atol=1e-10)
+    torch.testing.assert_close(Kx, Kd, rtol=0, atol=1e-10)
+    Ct = torch.tensor(C, device="cuda")
+    torch.testing.assert_close(torch.ops.slowquant_gb300.ao2mo(Ct, V),
+                               torch.einsum("ai,bj,ck,dl,abcd->ijkl", Ct, Ct, Ct, Ct, V), rtol=0, atol=1e-10)

@@ -434,3 +434,22 @@ def test_centre_of_mass_uses_the_reference_masses():
     for tag in ("h2o_631gs", "h2o2_ccpvtz"):
         m = molecule._Molecule(str(g[f"{tag}_geometry"]), 0, str(g[f"{tag}_unit"]))
         np.testing.assert_allclose(m.center_of_mass, g[f"{tag}_com"], atol=1e-12)
+
+
+def test_torch_operators_are_registered_with_shape_rules():
+    """torch.ops.slowquant_gb300.* exist and give output shapes on fake tensors (no device needed)."""
+    import torch
+    from torch._subclasses.fake_tensor import FakeTensorMode
+
+    import slowquant_gb300.torch_ops as ops
+
+    with FakeTensorMode():
+        V = torch.empty(6, 6, 6, 6, dtype=torch.float64)
+        D = torch.empty(6, 6, dtype=torch.float64)
+        J, K = torch.ops.slowquant_gb300.jk_dense(V, D)
+        assert J.shape == K.shape == (6, 6)
+        C = torch.empty(6, 4, dtype=torch.float64)
+        assert torch.ops.slowquant_gb300.ao2mo(C, V).shape == (4, 4, 4, 4)
+        J, K = torch.ops.slowquant_gb300.direct_jk(1, D, 1e-12, "fp64", 1e-4)
+        assert J.shape == (6, 6)
+    assert ops.register_engine(object()) >= 1
