@@ -30,7 +30,7 @@ extern "C" {
 #define SQ_MAX_L 3            /* highest shell angular momentum (f) of the ERI / J-K kernels */
 #define SQ_MAX_QCLASS 55      /* quartet classes for l <= SQ_MAX_L: 10 pair classes -> 55;
                                  classes 0-20 hold s, p, d shells only */
-#define SQ_MAX_L_GRAD 2       /* highest shell angular momentum of the gradient kernels */
+#define SQ_MAX_L_GRAD 3       /* highest shell angular momentum of the gradient kernels (f) */
 
 /* Boys-function grid, T_k = k / SQ_BOYS_STEP_INV, k < SQ_BOYS_NGRID.
  * FP64 table (SQ_BOYS_TAB64_SIZE doubles):

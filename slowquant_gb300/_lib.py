@@ -20,7 +20,7 @@ SQ_ERR_CUDA = 3
 SQ_ERR_NONFINITE = 4
 SQ_MAX_L = 3
 SQ_MAX_QCLASS = 55
-SQ_MAX_L_GRAD = 2
+SQ_MAX_L_GRAD = 3
 SQ_BOYS_NGRID = 580
 SQ_BOYS_STEP_INV = 16
 SQ_BOYS_NCOL = 16

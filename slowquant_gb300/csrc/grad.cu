@@ -25,16 +25,15 @@
 
 namespace sq {
 
-constexpr int kGradWarps = 4;
-constexpr int kGHmax = nherm(4 * SQ_LMAX + 1);                                    // R to L + 1
-constexpr int kGWmax = nherm(2 * SQ_LMAX + 1) * ncart(SQ_LMAX) * ncart(SQ_LMAX);  // W'[tuv][cd]
-constexpr int kGGmax = ncart(SQ_LMAX) * ncart(SQ_LMAX) * ncart(SQ_LMAX) * ncart(SQ_LMAX);
-constexpr int kGE = SQ_LMAX + 2;  // 1D tables with indices up to l + 1
+constexpr int kGradL = SQ_MAX_L_GRAD;       // f
+constexpr int kGradWarps = 4;               // warps per block where a class's slice fits four times
+constexpr int kGHmax = nherm(4 * kGradL + 1);  // R to L + 1
+constexpr int kGE = kGradL + 2;             // 1D tables with indices up to l + 1
 
 // A warp's shared-memory slice, laid out per quartet class (offsets in doubles):
 // two R buffers, W'[cd][h], Gamma'[ab][cd], the three 1D E tables, F_m.  Sizing
-// it per class (instead of for (dd|dd)) lets the light classes keep many more
-// warps resident.
+// it per class (instead of for (ff|ff)) lets the light classes keep many more
+// warps resident; an (ff|ff) slice (186 KB) runs one warp per block.
 struct GradLayout {
     int rbuf;    // entries per R buffer: nherm(L + 1)
     int W;       // offset of W'
@@ -71,9 +70,12 @@ __device__ inline void ecoef_table(double XPA, double XPB, double inv2p, int li,
         }
 }
 
-// F_m(T) for any m <= 15: the grid expansion while m + 6 <= 14, the
-// convergent series otherwise (only the top order of (dd|dd) gradients).
+// F_m(T) for any m <= 16: the Taylor grid while m + 6 <= 14, the high-order
+// grid above (the top orders of (dd|dd) and of every f class; it is exact to
+// T = 60, where the asymptote's neglected term for m = 13 is ~1e-13 relative,
+// against ~6e-6 at T = 36).
 __device__ inline double boys_any(int m, double T, const double *tab) {
+    if (m + kBoysTaylor64 - 1 > SQ_BOYS_NCOL - 2) return boys_hi(m, T, tab);
     if (T >= SQ_BOYS_TMAX) {
         const double r = rsqrt(T);
         double f = kSqrtPiHalf * r;
@@ -81,21 +83,12 @@ __device__ inline double boys_any(int m, double T, const double *tab) {
         for (int j = 0; j < m; ++j) f *= (2 * j + 1) * h;
         return f;
     }
-    if (m + kBoysTaylor64 - 1 <= SQ_BOYS_NCOL - 2) {
-        const int kk = __double2int_rn(T * SQ_BOYS_STEP_INV);
-        const double dd = T - kk * (1.0 / SQ_BOYS_STEP_INV);
-        const double *row = tab + kk * SQ_BOYS_NCOL + m;
-        double f = row[kBoysTaylor64 - 1];
-        for (int j = kBoysTaylor64 - 1; j >= 1; --j) f = fma(f, -dd / j, row[j - 1]);
-        return f;
-    }
-    double term = 1.0 / (2 * m + 1), sum = 0.0;
-    for (int i = 0; i < 400; ++i) {
-        sum += term;
-        term *= 2.0 * T / (2 * m + 2 * i + 3);
-        if (term < 1e-17 * sum) break;
-    }
-    return sum * exp(-T);
+    const int kk = __double2int_rn(T * SQ_BOYS_STEP_INV);
+    const double dd = T - kk * (1.0 / SQ_BOYS_STEP_INV);
+    const double *row = tab + kk * SQ_BOYS_NCOL + m;
+    double f = row[kBoysTaylor64 - 1];
+    for (int j = kBoysTaylor64 - 1; j >= 1; --j) f = fma(f, -dd / j, row[j - 1]);
+    return f;
 }
 
 cudaError_t launch_grad_thread_class(int qc, const EriArgs &a, int swap, double *grad, cudaStream_t s);
@@ -132,7 +125,7 @@ inline GradLayout grad_layout(int la, int lb, int lc, int ld) {
 __global__ void __launch_bounds__(32 * kGradWarps) grad2e_kernel(const EriArgs args, int swap, double *grad,
                                                                 const GradLayout lay) {
     extern __shared__ __align__(16) double smem_d[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
     double *wbase = smem_d + (long long)warp * lay.stride;
     double *rbuf0 = wbase, *rbuf1 = wbase + lay.rbuf;
     double *smW = wbase + lay.W, *smG = wbase + lay.G, *smFs = wbase + lay.Fs;
@@ -155,8 +148,8 @@ __global__ void __launch_bounds__(32 * kGradWarps) grad2e_kernel(const EriArgs a
     const sq_pairs &pr = args.pairs;
     const sq_basis &bs = args.basis;
     const long long n = bs.nbf;
-    const long long nwarps = (long long)gridDim.x * kGradWarps;
-    for (long long qi = (long long)blockIdx.x * kGradWarps + warp; qi < args.nq; qi += nwarps) {
+    const long long nwarps = (long long)gridDim.x * wpb;
+    for (long long qi = (long long)blockIdx.x * wpb + warp; qi < args.nq; qi += nwarps) {
         const int2 pq = args.quartets[qi];
         const int slotP = swap ? pq.y : pq.x, slotQ = swap ? pq.x : pq.y;
         const int P = gload(args.slots.pair + slotP), Q = gload(args.slots.pair + slotQ);
@@ -333,16 +326,18 @@ __global__ void __launch_bounds__(32 * kGradWarps) grad2e_kernel(const EriArgs a
 
 // ---------------------------------------------------------------------------
 // One-electron derivatives, one thread per shell pair (s1 >= s2).
-constexpr int kG1I = SQ_LMAX + 4;  // a + 1 + 2 for the kinetic operator
-constexpr int kG1J = SQ_LMAX + 2;
+constexpr int kG1I = kGradL + 4;  // a + 1 + 2 for the kinetic operator
+constexpr int kG1J = kGradL + 2;
+constexpr int kG1R = nherm(2 * kGradL + 1);  // R^0_{tuv} to L = la + lb + 1
 
-// R^0_{tuv}, t+u+v <= L (L <= 6), flat index ((t*7)+u)*7+v.
+// R^0_{tuv}, t+u+v <= L (L <= 2 kGradL + 1), at herm_index(t, u, v).
 __device__ inline void hermite_r_grad(int L, double p, const double *PC, const double *tab, double *out) {
-    double F[16];
+    double F[2 * kGradL + 2];
     const double T = p * (PC[0] * PC[0] + PC[1] * PC[1] + PC[2] * PC[2]);
     for (int m = 0; m <= L; ++m) F[m] = boys_any(m, T, tab);
-    double cur[343], nxt[343];
-#define RI(t, u, v) (((t) * 7 + (u)) * 7 + (v))
+    double bufa[kG1R], bufb[kG1R];
+    double *cur = bufa, *nxt = bufb;
+#define RI(t, u, v) herm_index(t, u, v)
     double fac = 1.0;
     for (int m = 0; m <= L; ++m) {
         F[m] *= fac;
@@ -369,13 +364,11 @@ __device__ inline void hermite_r_grad(int L, double p, const double *PC, const d
                     }
                     nxt[RI(t, u, v)] = val;
                 }
-        for (int t = 0; t <= top; ++t)
-            for (int u = 0; u <= top - t; ++u)
-                for (int v = 0; v <= top - t - u; ++v) cur[RI(t, u, v)] = nxt[RI(t, u, v)];
+        double *tmp = cur;
+        cur = nxt;
+        nxt = tmp;
     }
-    for (int t = 0; t <= L; ++t)
-        for (int u = 0; u <= L - t; ++u)
-            for (int v = 0; v <= L - t - u; ++v) out[RI(t, u, v)] = cur[RI(t, u, v)];
+    for (int e = 0; e < nherm(L); ++e) out[e] = cur[e];
 #undef RI
 }
 
@@ -403,7 +396,7 @@ __device__ inline double hermite_sum(const double (*E)[kG1I][kG1J][kG1I + kG1J],
     for (int t = 0; t <= a[0] + b[0]; ++t)
         for (int u = 0; u <= a[1] + b[1]; ++u)
             for (int v = 0; v <= a[2] + b[2]; ++v)
-                s += E[0][a[0]][b[0]][t] * E[1][a[1]][b[1]][u] * E[2][a[2]][b[2]][v] * R[(t * 7 + u) * 7 + v];
+                s += E[0][a[0]][b[0]][t] * E[1][a[1]][b[1]][u] * E[2][a[2]][b[2]][v] * R[herm_index(t, u, v)];
     return s;
 }
 
@@ -427,7 +420,7 @@ __global__ void grad1e_kernel(const sq_basis basis, const double *tab, const dou
     constexpr double pi = 3.141592653589793;
     double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0};
     double E[3][kG1I][kG1J][kG1I + kG1J];
-    double R[343];
+    double R[kG1R];
     for (int i = 0; i < np1; ++i)
         for (int j = 0; j < np2; ++j) {
             const double al = basis.exps[basis.prim_off[s1] + i], be = basis.exps[basis.prim_off[s2] + j];
@@ -542,9 +535,15 @@ extern "C" int sq_grad_2e(const sq_basis *basis, const sq_pairs *pairs, const sq
     a.D = D;
     a.quartets = reinterpret_cast<const int2 *>(quartets->pairs);
     a.nq = quartets->nquartet;
-    // one launch per quartet class and orientation, each with its own shared-memory layout
-    const size_t full = (size_t)grad_layout(SQ_LMAX, SQ_LMAX, SQ_LMAX, SQ_LMAX).stride * sizeof(double) * kGradWarps;
-    cudaError_t e = cudaFuncSetAttribute(grad2e_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)full);
+    // one launch per quartet class and orientation, each with its own shared-memory
+    // layout; as many warps per block (up to four) as the opt-in shared memory holds
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa{};
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, grad2e_kernel);
+    const long long avail = (long long)optin - (long long)fa.sharedSizeBytes;
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(grad2e_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)avail);
     if (e != cudaSuccess) return set_error(SQ_ERR_CUDA, "sq_grad_2e: %s", cudaGetErrorString(e));
     for (int c = 0; c < SQ_MAX_QCLASS; ++c) {
         const long long nq = quartets->class_off[c + 1] - quartets->class_off[c];
@@ -554,15 +553,21 @@ extern "C" int sq_grad_2e(const sq_basis *basis, const sq_pairs *pairs, const sq
         const GradLayout lay = grad_layout(la, lb, lc, ld);
         a.quartets = reinterpret_cast<const int2 *>(quartets->pairs) + quartets->class_off[c];
         a.nq = nq;
-        const size_t sz = (size_t)lay.stride * sizeof(double) * kGradWarps;
-        long long blocks = (nq + kGradWarps - 1) / kGradWarps;
+        const long long slice = (long long)lay.stride * (long long)sizeof(double);
+        long long wpb = avail / slice;
+        if (wpb > kGradWarps) wpb = kGradWarps;
+        if (wpb < 1)
+            return set_error(SQ_ERR_UNSUPPORTED, "sq_grad_2e: class %d needs %lld bytes of shared memory per warp", c,
+                             slice);
+        const size_t sz = (size_t)(slice * wpb);
+        long long blocks = (nq + wpb - 1) / wpb;
         if (blocks > sm_count() * 64) blocks = sm_count() * 64;
         for (int swap = 0; swap < 2; ++swap) {
             // light classes: one quartet per thread; the rest: one per warp
             if (grad_thread_enabled() &&
                 launch_grad_thread_class(c, a, swap, grad, (cudaStream_t)stream) != cudaErrorNotSupported)
                 continue;
-            grad2e_kernel<<<(unsigned)blocks, 32 * kGradWarps, sz, (cudaStream_t)stream>>>(a, swap, grad, lay);
+            grad2e_kernel<<<(unsigned)blocks, (unsigned)(32 * wpb), sz, (cudaStream_t)stream>>>(a, swap, grad, lay);
         }
     }
     return check_launch("sq_grad_2e");

@@ -6,7 +6,6 @@ generic in l; cc-pVTZ puts f shells on O.  Tolerances as for s/p/d: integrals
 tensor, FP32 paths within the FP32 error scale.
 """
 
-import ctypes
 
 import numpy as np
 import pytest
@@ -236,29 +235,6 @@ def test_batch_with_f_shells(gpu_lib):
         log.print_output = False
         ref.append(run_hartree_fock(S, T, V, DirectJK(eng), m.number_electrons, log, 1e-10, 1e-10, 100, True)[0])
     np.testing.assert_allclose(E, np.array(ref), atol=1e-8)
-
-
-def test_gradient_refuses_f_shells(h2o2):
-    """No gradient kernel for f: the Python layer and both C entry points refuse, nothing runs."""
-    import torch
-
-    from slowquant_gb300 import _lib
-
-    e, eng = h2o2
-    D = torch.zeros((eng.nbf, eng.nbf), dtype=torch.float64, device="cuda")
-    with pytest.raises(NotImplementedError):
-        eng.nuclear_gradient(D)
-    grad = torch.zeros((len(eng.mol.atoms), 3), dtype=torch.float64, device="cuda")
-    lib = _lib.lib()
-    rc = lib.sq_grad_1e(ctypes.byref(eng.cbasis), eng.tab64.data_ptr(), D.data_ptr(), D.data_ptr(),
-                        grad.data_ptr(), _lib.stream_handle())
-    assert rc == _lib.SQ_ERR_UNSUPPORTED
-    qs = eng.quartets(1e-12, split=False).cstruct()
-    rc = lib.sq_grad_2e(ctypes.byref(eng.cbasis), ctypes.byref(eng.cpairs), ctypes.byref(eng.slots),
-                        ctypes.byref(qs), eng.tab64.data_ptr(), D.data_ptr(), grad.data_ptr(),
-                        _lib.stream_handle())
-    assert rc == _lib.SQ_ERR_UNSUPPORTED
-    assert float(grad.abs().sum()) == 0.0
 
 
 def test_f_classes_agree_across_kernel_shapes(h2o2):

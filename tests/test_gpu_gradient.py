@@ -58,6 +58,39 @@ def test_water_gradient_matches_fd_of_reference_energies(basis, gpu_lib):
     np.testing.assert_allclose(g.sum(axis=0), 0.0, atol=1e-8)
 
 
+def test_f_shell_gradient_matches_fd_of_reference_energies(gpu_lib):
+    """cc-pVTZ puts f shells on O: every f class of the adjoint kernels, (ff|ff)
+    on one-warp blocks, the high-order Boys grid for m > 8 and the
+    one-electron kernel at l = 3, against finite differences of the oracle."""
+    symbols = [s for s, _ in H2O_BOHR]
+    xyz = [list(c) for _, c in H2O_BOHR]
+    xyz[1][2] += 0.05
+    g = gpu_gradient(symbols, xyz, "cc-pvtz")
+    fd = fd_gradient(symbols, xyz, "cc-pvtz")
+    np.testing.assert_allclose(g, fd, atol=1e-6)
+    np.testing.assert_allclose(g.sum(axis=0), 0.0, atol=1e-8)
+
+
+def test_f_shell_gradient_per_thread_classes_match_warp_kernel(gpu_lib):
+    """With f shells present, the light classes on per-thread kernels == all on the warp kernel."""
+    from slowquant_gb300 import _lib
+    from slowquant_gb300.gradient import molecule_from_coords, rhf_gradient
+
+    symbols = [s for s, _ in H2O_BOHR]
+    xyz = [list(c) for _, c in H2O_BOHR]
+    xyz[2][2] -= 0.03
+    m = molecule_from_coords(symbols, xyz, "cc-pvtz")
+    L = _lib.lib()
+    try:
+        _lib.check(L.sq_set_option(_lib.SQ_OPT_GRAD_THREAD, 0), "sq_set_option")
+        g_warp = rhf_gradient(m, conv=1e-11)
+        _lib.check(L.sq_set_option(_lib.SQ_OPT_GRAD_THREAD, 1), "sq_set_option")
+        g_thread = rhf_gradient(m, conv=1e-11)
+    finally:
+        L.sq_set_option(_lib.SQ_OPT_GRAD_THREAD, 1)
+    np.testing.assert_allclose(g_thread, g_warp, atol=1e-10)
+
+
 def test_water_dimer_gradient_multicentre(gpu_lib):
     from slowquant_gb300 import systems
     from slowquant_gb300.molecule import ANGSTROM_TO_BOHR
