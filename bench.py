@@ -460,6 +460,43 @@ def gpu_arm(args) -> None:
                            "fp32_list_quartets": p32.nquartet,
                            "mixed_builds": sum(1 for b in jkp.builds if b != "fp64"), "builds": len(jkp.builds)})
 
+    # double-float arithmetic on the FP32 pipe (sq_jk_df) in place of FP64: the
+    # whole build, then the primitive-level mixed mode with double-float above the bound
+    df_full, df_modes = None, []
+    if args.df:
+        eng.fock(H, D, SCREEN, "df64")
+        torch.cuda.nvtx.range_push("timed_df64")
+        ms_df = float(np.median(time_events(torch, lambda: eng.fock(H, D, SCREEN, "df64"), 5, flush)))
+        torch.cuda.nvtx.range_pop()
+        Fd = eng.fock(H, D, SCREEN, "df64")
+        jkd = DirectJK(eng, SCREEN, "df64")
+        Ed, _, _, _ = run_hartree_fock(S, T, V, jkd, ne, log, 1e-9, 1e-9, 100, True)
+        J64, K64 = eng.jk(D, SCREEN, "fp64")
+        Jd, Kd = eng.jk(D, SCREEN, "df64")
+        df_full = {"fock_build_ms": ms_df, "speedup_vs_fp64": ms64 / ms_df,
+                   "dE_one_build": float(0.5 * torch.sum(D * (H + Fd))) - E_build64, "dE_scf": Ed - E64,
+                   "dE_scf_vs_oracle": None if orc is None else Ed - orc["E_hf"],
+                   "max_abs_dJ_vs_fp64": float((Jd - J64).abs().max()),
+                   "max_abs_dK_vs_fp64": float((Kd - K64).abs().max()), "builds": len(jkd.builds)}
+        for tau in args.prim_sweep:
+            eng.fock(H, D, SCREEN, "mixed_df", tau)
+            torch.cuda.nvtx.range_push(f"timed_mixed_df_{tau:g}")
+            ms_q = float(np.median(time_events(torch, lambda: eng.fock(H, D, SCREEN, "mixed_df", tau), 5, flush)))
+            torch.cuda.nvtx.range_pop()
+            Fq = eng.fock(H, D, SCREEN, "mixed_df", tau)
+            jkq = DirectJK(eng, SCREEN, "mixed_df", tau, 1e-5)
+            Eq, _, _, _ = run_hartree_fock(S, T, V, jkq, ne, log, 1e-9, 1e-9, 100, True)
+            d64, _ = eng.quartets(SCREEN, tau)
+            eng.jk_accumulate(D, [d64], ["df64_prim"], prim_tau=tau)
+            ms_d64 = float(np.median(time_events(
+                torch, lambda: eng.jk_accumulate(D, [d64], ["df64_prim"], prim_tau=tau), 5, flush)))
+            df_modes.append({"fp32_threshold": tau, "fock_build_ms": ms_q, "speedup_vs_fp64": ms64 / ms_q,
+                             "dE_one_build": float(0.5 * torch.sum(D * (H + Fq))) - E_build64, "dE_scf": Eq - E64,
+                             "dE_scf_vs_oracle": None if orc is None else Eq - orc["E_hf"],
+                             "df64_list_alone_ms": ms_d64,
+                             "mixed_builds": sum(1 for b in jkq.builds if b == "mixed_df"),
+                             "builds": len(jkq.builds)})
+
     # launch shapes from the project's autotuner on this workload's lists, timed beside the defaults
     tuned = None
     if args.autotune:
@@ -582,6 +619,8 @@ def gpu_arm(args) -> None:
         "tau_sweep": sweep,
         "chunk_precision": chunk_modes,
         "prim_precision": prim_modes,
+        "df64": df_full,
+        "mixed_df": df_modes,
         "autotuned_launch_shapes": tuned,
         "kernels_by_time": rows[:8],
         "fp32_kernels_by_time": [r for r in rows if r["precision"] == "fp32"][:8],
@@ -770,6 +809,8 @@ def main() -> None:
                     help="also time the build with the autotuner's launch shapes for this workload")
     ap.add_argument("--prim-sweep", type=float, nargs="*", default=[1e-4, 1e-3, 1e-2],
                     help="bounds of the primitive-level precision mode reported beside the headline (empty: skip)")
+    ap.add_argument("--no-df", dest="df", action="store_false",
+                    help="skip the double-float (df64, mixed_df) measurements")
     args = ap.parse_args()
     global WATERS, SEED, BASIS
     WATERS = SEED = args.waters

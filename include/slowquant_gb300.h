@@ -42,7 +42,10 @@ extern "C" {
  *     HI_NCOL-1 = exp(-T_k).  Same step; tabulated to SQ_BOYS_HI_TMAX.
  * FP32 table (SQ_BOYS_TAB32_SIZE floats): the same F grid, then
  *   [SQ_BOYS_TAY32_OFF + (m*NGRID + k)*4 + j], j < 4, and the fifth
- *   coefficient (j = 4) at [SQ_BOYS_TAY32_5_OFF + m*NGRID + k]. */
+ *   coefficient (j = 4) at [SQ_BOYS_TAY32_5_OFF + m*NGRID + k], then the
+ *   double-float Taylor rows of the df64 kernels: 12 floats per (m, k) at
+ *   [SQ_BOYS_DF_OFF + (m*NGRID + k)*12]: coefficients 0-3 as (hi, lo) pairs,
+ *   4-6 as floats, one pad. */
 #define SQ_BOYS_NGRID 580
 #define SQ_BOYS_STEP_INV 16
 #define SQ_BOYS_NCOL 16
@@ -55,7 +58,8 @@ extern "C" {
 #define SQ_BOYS_TAB64_SIZE (SQ_BOYS_HI64_OFF + SQ_BOYS_HI_NGRID * SQ_BOYS_HI_NCOL)
 #define SQ_BOYS_TAY32_OFF (SQ_BOYS_NGRID * SQ_BOYS_NCOL)
 #define SQ_BOYS_TAY32_5_OFF (SQ_BOYS_TAY32_OFF + 16 * SQ_BOYS_NGRID * 4)
-#define SQ_BOYS_TAB32_SIZE (SQ_BOYS_TAY32_5_OFF + 16 * SQ_BOYS_NGRID)
+#define SQ_BOYS_DF_OFF (SQ_BOYS_TAY32_5_OFF + 16 * SQ_BOYS_NGRID)
+#define SQ_BOYS_TAB32_SIZE (SQ_BOYS_DF_OFF + 16 * SQ_BOYS_NGRID * 12)
 
 /* Precision of one ERI / J-K launch. */
 #define SQ_FP64 0             /* all arithmetic in FP64 */
@@ -63,6 +67,8 @@ extern "C" {
 #define SQ_FP32_BOYS32 2      /* FP32 integral arithmetic and FP32 Boys function */
 #define SQ_FP64_PRIM 3        /* FP64 with primitive-level precision (sq_jk_prim only): primitive
                                  quartets with q_ij q_kl below a bound run as in SQ_FP32 */
+#define SQ_DF64 4             /* double-float arithmetic on the FP32 pipe (sq_jk_df only), with the
+                                 same primitive-level split as SQ_FP64_PRIM */
 
 /* Contracted Cartesian Gaussian shells of one molecule (device arrays).
  * Replaces the per-shell Python objects of slowquant/molecule/moleculeclass.py:269-301. */
@@ -165,6 +171,13 @@ typedef struct sq_slots {
      * pair at prim32v[8 (pbase + k pstride) + f], f = p, Px, Py, Pz, U, the
      * primitive Schwarz factor (0 when pairs->pq is NULL), 0, 0. */
     float *prim32v;
+    /* Double-float copies for SQ_DF64 launches (sq_jk_df; written by
+     * sq_slots_fill when non-NULL): every value v as the float pair (hi, lo),
+     * hi = (float)v, lo = (float)(v - hi); primdf holds 2 * 5 * npp_total floats
+     * laid out like prim (pair index f * npp_total + i), hermdf 2 * nherm_total
+     * floats laid out like herm. */
+    float *primdf;
+    float *hermdf;
 } sq_slots;
 
 /* Shell-quartet work list: device array of (bra pair, ket pair) index pairs,
@@ -205,6 +218,12 @@ const char *sq_last_error(void);
  * ((ss|ss), (ps|ss), (ps|ps), (pp|ss), (pp|ps), (ds|ss), (ds|ps), (dp|ss))
  * one quartet per thread, 0 one quartet per warp like the other classes. */
 #define SQ_OPT_GRAD_THREAD 4
+/* SQ_OPT_DF_CLASSES: bit mask over quartet classes 0-18; a set bit runs the
+ * class's SQ_DF64 launches (sq_jk_df) on its double-float kernel, a clear bit
+ * as in sq_jk_prim (FP64 with the primitive split where the class has it).
+ * Default: the classes where double-float measured faster, SQ_DF_CLASSES_DEFAULT. */
+#define SQ_OPT_DF_CLASSES 5
+#define SQ_DF_CLASSES_DEFAULT 0x7FFFFLL
 int sq_set_option(int key, long long value);
 long long sq_get_option(int key);
 
@@ -302,6 +321,21 @@ int sq_jk_multi(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *sl
 int sq_jk_prim(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, const sq_quartets *quartets,
                const double *table64, const float *table32, const double *D, double *Jacc, double *Kacc,
                double prim_tau, void *stream);
+
+/* Double-float J/K build (no counterpart in the reference).  Like sq_jk_prim,
+ * except that the classes (ss|ss) to (dd|ds) carry every FP64 quantity as a
+ * pair of floats (hi + lo, about 46 significant bits) and do all their
+ * arithmetic on the FP32 pipe, which GB300 runs at about 60 times its FP64
+ * rate; Boys values come from the double-float rows of table32
+ * (SQ_BOYS_DF_OFF).  prim_tau splits as in sq_jk_prim (0: every primitive
+ * quartet in double-float).  Ddf is caller scratch of 2 * nbf * nbf floats
+ * (mat_total pairs for a packed basis) that the call fills with D as
+ * double-float pairs; slots->primdf and slots->hermdf must be written (by
+ * sq_slots_fill).  The classes without a double-float kernel run as in
+ * sq_jk_prim.  J/K accumulate in FP64. */
+int sq_jk_df(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, const sq_quartets *quartets,
+             const double *table64, const float *table32, const double *D, float *Ddf, double *Jacc, double *Kacc,
+             double prim_tau, void *stream);
 
 /* J/K build for callers that cannot allocate device memory.  No counterpart
  * in the reference (it has no device code).  Same arguments and results as

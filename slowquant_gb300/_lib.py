@@ -28,22 +28,28 @@ SQ_BOYS_TMAX = 36.0
 SQ_BOYS_HI_NGRID = 968
 SQ_BOYS_HI_NCOL = 24
 SQ_BOYS_HI_TMAX = 60.0
-SQ_BOYS_HI64_OFF = SQ_BOYS_NGRID * SQ_BOYS_NCOL + 16 * SQ_BOYS_NGRID * 8
+SQ_BOYS_TAY64_OFF = SQ_BOYS_NGRID * SQ_BOYS_NCOL
+SQ_BOYS_HI64_OFF = SQ_BOYS_TAY64_OFF + 16 * SQ_BOYS_NGRID * 8
 SQ_BOYS_TAB64_SIZE = SQ_BOYS_HI64_OFF + SQ_BOYS_HI_NGRID * SQ_BOYS_HI_NCOL
 SQ_BOYS_TAY32_5_OFF = SQ_BOYS_NGRID * SQ_BOYS_NCOL + 16 * SQ_BOYS_NGRID * 4
-SQ_BOYS_TAB32_SIZE = SQ_BOYS_TAY32_5_OFF + 16 * SQ_BOYS_NGRID
+SQ_BOYS_DF_OFF = SQ_BOYS_TAY32_5_OFF + 16 * SQ_BOYS_NGRID
+SQ_BOYS_TAB32_SIZE = SQ_BOYS_DF_OFF + 16 * SQ_BOYS_NGRID * 12
 SQ_FP64 = 0
 SQ_FP32 = 1
 SQ_FP32_BOYS32 = 2
 SQ_FP64_PRIM = 3
+SQ_DF64 = 4
 SQ_OPT_GENERIC_MIN_L = 1
 SQ_OPT_JK_STREAMS = 2
 SQ_OPT_FP64_UNROLLED_HIGH = 3
 SQ_OPT_GRAD_THREAD = 4
+SQ_OPT_DF_CLASSES = 5
+SQ_DF_CLASSES_DEFAULT = 0x7FFFF
 SQ_NOALLOC_MAX_NBF = 1024
 SQ_NOALLOC_MAX_ELEMS = SQ_NOALLOC_MAX_NBF * SQ_NOALLOC_MAX_NBF
 
-PRECISIONS = {"fp64": SQ_FP64, "fp32": SQ_FP32, "fp32_boys32": SQ_FP32_BOYS32, "fp64_prim": SQ_FP64_PRIM}
+PRECISIONS = {"fp64": SQ_FP64, "fp32": SQ_FP32, "fp32_boys32": SQ_FP32_BOYS32, "fp64_prim": SQ_FP64_PRIM,
+              "df64": SQ_DF64}
 
 _p = ctypes.c_void_p
 
@@ -70,6 +76,7 @@ class SqSlots(ctypes.Structure):
         ("pair", _p), ("npp", _p), ("pbase", _p), ("pstride", _p), ("hbase", _p),
         ("prim", _p), ("herm", _p), ("prim32", _p), ("herm32", _p),
         ("prim_src", _p), ("prim_src_off", _p), ("sub", _p), ("desc", _p), ("mbase", _p), ("prim32v", _p),
+        ("primdf", _p), ("hermdf", _p),
     ]
 
 
@@ -140,6 +147,8 @@ def lib() -> ctypes.CDLL:
         L.sq_jk_dense.argtypes = [ctypes.c_int, _p, _p, _p, _p, _p]
         L.sq_jk_prim.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
                                  ctypes.POINTER(SqQuartets), _p, _p, _p, _p, _p, ctypes.c_double, _p]
+        L.sq_jk_df.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
+                               ctypes.POINTER(SqQuartets), _p, _p, _p, _p, _p, _p, ctypes.c_double, _p]
         L.sq_jk_noalloc.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
                                     ctypes.POINTER(SqQuartets), _p, _p, _p, _p, _p, ctypes.c_int, _p]
         L.sq_fock_build.argtypes = [ctypes.c_int, _p, _p, _p, _p, _p, _p, _p]
@@ -155,7 +164,7 @@ def lib() -> ctypes.CDLL:
 EXPORTED = [
     "sq_version", "sq_last_error", "sq_set_option", "sq_get_option", "sq_set_launch_config", "sq_boys_table", "sq_boys",
     "sq_pair_prep", "sq_schwarz", "sq_eri_dense", "sq_jk", "sq_fock_build", "sq_one_electron",
-    "sq_quartets_expand", "sq_fma_probe", "sq_slots_fill", "sq_slots_describe", "sq_jk_prim", "sq_ao2mo_rotate", "sq_multipole", "sq_jk_dense", "sq_jk_noalloc", "sq_grad_2e", "sq_grad_1e",
+    "sq_quartets_expand", "sq_fma_probe", "sq_slots_fill", "sq_slots_describe", "sq_jk_prim", "sq_jk_df", "sq_ao2mo_rotate", "sq_multipole", "sq_jk_dense", "sq_jk_noalloc", "sq_grad_2e", "sq_grad_1e",
     "sq_batched_eigh", "sq_jk_multi",
 ]
 

@@ -23,6 +23,7 @@
 // tolerance on integrals.
 #pragma once
 
+#include "df64.cuh"
 #include "sq_common.cuh"
 
 namespace sq {
@@ -81,6 +82,52 @@ __device__ __forceinline__ void boys64(double T, const double *__restrict__ tab,
             const double h = 0.5 * r * r;  // 1/(2T)
 #pragma unroll
             for (int m = 0; m < M; ++m) F[m + 1] = F[m] * ((2 * m + 1) * h);
+        }
+    }
+}
+
+// Taylor sum of one double-float row (SQ_BOYS_DF_OFF) at md = T_k - T:
+// coefficients 4-6 in FP32 (their terms are below 4e-8 of the sum for
+// |md| <= 1/32, so FP32 rounding there stays near 2^-48 of the result), 0-3
+// in double-float.
+__device__ __forceinline__ dfl taylor_df(const float4 *__restrict__ row, dfl md) {
+    const float4 a = __ldg(row), b = __ldg(row + 1), c = __ldg(row + 2);
+    const float g = __fmaf_rn(__fmaf_rn(c.z, md.hi, c.y), md.hi, c.x);
+    dfl f = fma(dfl(g), md, dfl(b.z, b.w));
+    f = fma(f, md, dfl(b.x, b.y));
+    f = fma(f, md, dfl(a.z, a.w));
+    return fma(f, md, dfl(a.x, a.y));
+}
+
+// Double-float F[0..M] at T >= 0 (the df64 J/K kernels), the scheme of boys64
+// on the FP32 pipe.  tab: the double-float rows (float4 view of
+// table32 + SQ_BOYS_DF_OFF).  md = T_k - T is exact in its high part
+// (k/16 and T.hi are within a factor of two of each other for k >= 1).
+template <int M>
+__device__ __forceinline__ void boys_df(dfl T, const float4 *__restrict__ tab, dfl (&F)[M + 1]) {
+    static_assert(M + kBoysTaylor64 <= SQ_BOYS_NCOL - 1, "Boys table too narrow for this order");
+    if (T.hi < (float)SQ_BOYS_TMAX) {
+        const int k = __float2int_rn(__fmul_rn(T.hi, (float)SQ_BOYS_STEP_INV));
+        const dfl md = df_two_sum(__fsub_rn(__fmul_rn((float)k, 1.0f / SQ_BOYS_STEP_INV), T.hi), -T.lo);
+        const float4 *tay = tab + (long long)k * 3;
+        if constexpr (M <= 1) {
+#pragma unroll
+            for (int m = 0; m <= M; ++m) F[m] = taylor_df(tay + m * SQ_BOYS_NGRID * 3, md);
+        } else {
+            F[M] = taylor_df(tay + M * SQ_BOYS_NGRID * 3, md);
+            const dfl e = taylor_df(tay + 15 * SQ_BOYS_NGRID * 3, md);
+            const dfl T2(__fadd_rn(T.hi, T.hi), __fadd_rn(T.lo, T.lo));
+#pragma unroll
+            for (int m = M - 1; m >= 0; --m) F[m] = fma(T2, F[m + 1], e) * dfl(1.0 / (2 * m + 1));
+        }
+    } else {
+        const dfl r = rsqrt_df(T);
+        F[0] = dfl(kSqrtPiHalf) * r;
+        if constexpr (M >= 1) {
+            const dfl r2 = r * r;
+            const dfl h(__fmul_rn(0.5f, r2.hi), __fmul_rn(0.5f, r2.lo));  // 1/(2T)
+#pragma unroll
+            for (int m = 0; m < M; ++m) F[m + 1] = df_mul(F[m] * h, (float)(2 * m + 1));
         }
     }
 }

@@ -47,6 +47,19 @@ cudaError_t launch_eri_block(const EriArgs &, int, int, int, int, int, int, cuda
 #define DECL64(QC) cudaError_t launch_qc_##QC##_f64(const EriArgs &, int, int, cudaStream_t);
 DECL64(12) DECL64(13) DECL64(14) DECL64(15) DECL64(16) DECL64(17) DECL64(18)
 #undef DECL64
+#define DECLDF(QC) cudaError_t launch_qc_##QC##_df(const EriArgs &, int, int, cudaStream_t);
+DECLDF(0) DECLDF(1) DECLDF(2) DECLDF(3) DECLDF(4) DECLDF(5) DECLDF(6) DECLDF(7) DECLDF(8) DECLDF(9) DECLDF(10)
+DECLDF(11) DECLDF(12) DECLDF(13) DECLDF(14) DECLDF(15) DECLDF(16) DECLDF(17) DECLDF(18)
+#undef DECLDF
+
+// Double-float (SQ_DF64) per-thread kernels of classes 0-18, (ss|ss) to
+// (dd|ds): the classes of the s, p, d per-thread kernels.
+static const eri_launcher kLaunchersDF[SQ_MAX_QCLASS] = {
+    launch_qc_0_df,  launch_qc_1_df,  launch_qc_2_df,  launch_qc_3_df,  launch_qc_4_df,  launch_qc_5_df,
+    launch_qc_6_df,  launch_qc_7_df,  launch_qc_8_df,  launch_qc_9_df,  launch_qc_10_df, launch_qc_11_df,
+    launch_qc_12_df, launch_qc_13_df, launch_qc_14_df, launch_qc_15_df, launch_qc_16_df, launch_qc_17_df,
+    launch_qc_18_df, nullptr,         nullptr,
+};
 
 // FP64 (SQ_FP64) per-thread kernels of classes 12-18, (dp|pp) to (dd|ds): their
 // register blocks spill partly to local memory, and they still outrun the
@@ -93,6 +106,8 @@ static int g_generic_min_l = 5;
 // Bit c set: the FP64 J/K launches of class c run on its kLaunchersF64 kernel,
 // else on the warp kernel (option SQ_OPT_FP64_UNROLLED_HIGH).
 static long long g_fp64_unrolled_high = 0x7FLL << 12;  // classes 12-18
+// Bit c set: SQ_DF64 launches of class c run on its double-float kernel (option SQ_OPT_DF_CLASSES).
+static long long g_df_classes = SQ_DF_CLASSES_DEFAULT;
 // Per-thread gradient kernels for the light classes (option SQ_OPT_GRAD_THREAD).
 static int g_grad_thread = 1;
 int grad_thread_enabled() { return g_grad_thread; }
@@ -184,6 +199,13 @@ static cudaError_t launch_class(EriArgs &args, const sq_quartets *qs, int c, int
     if (mode == MODE_JK && (precision == SQ_FP64 || precision == SQ_FP64_PRIM) && kLaunchersF64[c] != nullptr &&
         g_generic_min_l > 0 && ((g_fp64_unrolled_high >> c) & 1))
         unrolled = kLaunchersF64[c];
+    // SQ_DF64 runs on the double-float kernels where a class has one, else as
+    // SQ_FP64_PRIM (which keeps the per-thread f classes' split)
+    if (mode == MODE_JK && precision == SQ_DF64) {
+        if (kLaunchersDF[c] != nullptr && g_generic_min_l > 0 && ((g_df_classes >> c) & 1))
+            return kLaunchersDF[c](args, mode, precision, stream);
+        return launch_class(args, qs, c, mode, SQ_FP64_PRIM, stream);
+    }
     // SQ_FP64_PRIM reaches only the per-thread kernels of kLaunchers; every
     // other kernel runs such a launch as plain FP64
     const int plain = precision == SQ_FP64_PRIM ? SQ_FP64 : precision;
@@ -264,6 +286,12 @@ extern "C" int sq_set_option(int key, long long value) {
         g_fp64_unrolled_high = value;
         return SQ_OK;
     }
+    if (key == SQ_OPT_DF_CLASSES) {
+        if (value < 0 || value >= (1LL << SQ_MAX_QCLASS))
+            return set_error(SQ_ERR_ARG, "sq_set_option: class mask out of range");
+        g_df_classes = value;
+        return SQ_OK;
+    }
     if (key == SQ_OPT_GENERIC_MIN_L) {
         if (value < 0) return set_error(SQ_ERR_ARG, "sq_set_option: negative L");
         g_generic_min_l = (int)value;
@@ -286,6 +314,7 @@ extern "C" long long sq_get_option(int key) {
     if (key == SQ_OPT_JK_STREAMS) return g_jk_streams;
     if (key == SQ_OPT_FP64_UNROLLED_HIGH) return g_fp64_unrolled_high;
     if (key == SQ_OPT_GRAD_THREAD) return g_grad_thread;
+    if (key == SQ_OPT_DF_CLASSES) return g_df_classes;
     return -1;
 }
 
@@ -322,7 +351,7 @@ extern "C" int sq_eri_dense(const sq_basis *basis, const sq_pairs *pairs, const 
 static int jk_common(const char *who, const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots,
                      const sq_quartets *quartets, const double *table64, const float *table32, int nd,
                      const double *D, float *D32, double *Jacc, double *Kacc, int precision, void *stream,
-                     bool pooled = true, float prim_tau = 0.0f) {
+                     bool pooled = true, float prim_tau = 0.0f, float *Ddf = nullptr) {
     int rc = check_common(who, basis, pairs, quartets, table64);
     if (rc) return rc;
     if (!slots || !slots->prim || !slots->herm || !slots->pair || !slots->desc)
@@ -331,17 +360,24 @@ static int jk_common(const char *who, const sq_basis *basis, const sq_pairs *pai
         return set_error(SQ_ERR_ARG, "%s: a packed batch basis needs slots->mbase", who);
     if (!D || !Jacc || !Kacc) return set_error(SQ_ERR_ARG, "%s: D, Jacc and Kacc are required", who);
     if (nd < 1) return set_error(SQ_ERR_ARG, "%s: nd = %d densities", who, nd);
-    if (precision != SQ_FP64 && precision != SQ_FP32 && precision != SQ_FP32_BOYS32 && precision != SQ_FP64_PRIM)
+    if (precision != SQ_FP64 && precision != SQ_FP32 && precision != SQ_FP32_BOYS32 && precision != SQ_FP64_PRIM &&
+        precision != SQ_DF64)
         return set_error(SQ_ERR_ARG, "%s: unknown precision %d", who, precision);
-    if (precision == SQ_FP64_PRIM &&
+    if ((precision == SQ_FP64_PRIM || precision == SQ_DF64) &&
         (!pairs->pq || !slots->prim32v || !slots->herm32 || !table32 || !(prim_tau >= 0.0f)))
         return set_error(SQ_ERR_ARG, "%s: primitive-level precision needs pairs->pq, FP32 slot data, table32 and a "
                          "non-negative bound", who);
+    if (precision == SQ_DF64 && (!Ddf || !slots->primdf || !slots->hermdf))
+        return set_error(SQ_ERR_ARG, "%s: double-float launches need Ddf and slots->primdf, slots->hermdf", who);
     cudaStream_t s = (cudaStream_t)stream;
     const long long mt = mat_total(*basis);
     if (mt >= (1LL << 31))
         return set_error(SQ_ERR_ARG, "%s: %lld matrix elements exceed the kernels' 32-bit indexing", who, mt);
-    if (precision != SQ_FP64 && precision != SQ_FP64_PRIM) {
+    if (precision == SQ_DF64) {
+        rc = to_df(mt * nd, D, Ddf, s);
+        if (rc) return rc;
+    }
+    if (precision != SQ_FP64 && precision != SQ_FP64_PRIM && precision != SQ_DF64) {
         if (!D32 || !pairs->prim32 || !pairs->herm32 || !slots->prim32 || !slots->herm32 || !slots->prim32v ||
             !table32)
             return set_error(SQ_ERR_ARG, "%s: FP32 precision needs D32, FP32 pair/slot data and table32", who);
@@ -362,6 +398,7 @@ static int jk_common(const char *who, const sq_basis *basis, const sq_pairs *pai
     a.Jacc = Jacc;
     a.Kacc = Kacc;
     a.prim_tau = prim_tau;
+    a.Ddf = Ddf;
     return run_classes(who, a, quartets, MODE_JK, precision, s, pooled);
 }
 
@@ -386,6 +423,13 @@ extern "C" int sq_jk_prim(const sq_basis *basis, const sq_pairs *pairs, const sq
                           double *Jacc, double *Kacc, double prim_tau, void *stream) {
     return jk_common("sq_jk_prim", basis, pairs, slots, quartets, table64, table32, 1, D, nullptr, Jacc, Kacc,
                      SQ_FP64_PRIM, stream, true, (float)prim_tau);
+}
+
+extern "C" int sq_jk_df(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots,
+                        const sq_quartets *quartets, const double *table64, const float *table32, const double *D,
+                        float *Ddf, double *Jacc, double *Kacc, double prim_tau, void *stream) {
+    return jk_common("sq_jk_df", basis, pairs, slots, quartets, table64, table32, 1, D, nullptr, Jacc, Kacc,
+                     SQ_DF64, stream, true, (float)prim_tau, Ddf);
 }
 
 extern "C" int sq_jk_multi(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots,

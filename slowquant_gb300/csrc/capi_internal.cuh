@@ -15,6 +15,7 @@ int check_launch(const char *what);
 
 // y[i] = (float)x[i] on `stream`.
 int to_float(long long n, const double *x, float *y, cudaStream_t stream);
+int to_df(long long n, const double *x, float *y, cudaStream_t stream);
 
 // sq_jk with every class launch on the caller's stream (no library stream pool).
 int jk_serial(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots, const sq_quartets *quartets,

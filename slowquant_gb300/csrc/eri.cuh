@@ -24,6 +24,7 @@
 #include <type_traits>
 
 #include "boys.cuh"
+#include "df64.cuh"
 #include "sq_common.cuh"
 
 namespace sq {
@@ -50,8 +51,12 @@ struct EriArgs {
     long long cfg_blocks;
     int nd;                 // J/K: densities digested per integral (0 or 1: one)
     long long dstride;      // elements between consecutive densities / accumulators
-    float prim_tau;         // SQ_FP64_PRIM launches: primitive quartets with q_ij q_kl < prim_tau run in FP32
+    float prim_tau;         // SQ_FP64_PRIM / SQ_DF64 launches: primitive quartets with q_ij q_kl < prim_tau run in FP32
+    const float *Ddf;       // SQ_DF64: the density as (hi, lo) float pairs
 };
+
+template <typename R>
+constexpr bool is_df = std::is_same<R, dfl>::value;
 
 constexpr double kTwoPi52 = 34.98683665524972;  // 2 pi^{5/2}
 
@@ -81,6 +86,8 @@ template <typename R>
 __device__ __forceinline__ const R *slot_herm_ptr(const sq_slots &sl) {
     if constexpr (std::is_same<R, double>::value)
         return sl.herm;
+    else if constexpr (is_df<R>)
+        return reinterpret_cast<const dfl *>(sl.hermdf);
     else
         return sl.herm32;
 }
@@ -103,6 +110,8 @@ template <typename R>
 __device__ __forceinline__ R rsqrt_r(R x) {
     if constexpr (std::is_same<R, double>::value)
         return rsqrt_f64(x);
+    else if constexpr (is_df<R>)
+        return rsqrt_df(x);
     else
         return rsqrtf(x);
 }
@@ -154,7 +163,10 @@ __device__ __forceinline__ void hermite_r(const R (&Fs)[L + 1], R X, R Y, R Z, R
 
 template <typename T>
 __device__ __forceinline__ T gload(const T *p) {
-    return __ldg(p);
+    if constexpr (is_df<T>)
+        return df_load(p);
+    else
+        return __ldg(p);
 }
 
 // Per-slot descriptor (sq_slots::desc): primitive-pair layout of the slot and
@@ -194,14 +206,19 @@ struct PrimPair {
     R p, x, y, z, u;
 };
 
-// FP64 reads the field-major arrays (five coalesced loads), FP32 the packed
-// copy (one 16-byte load plus one 4-byte load).
+// FP64 and double-float read the field-major arrays (five coalesced loads),
+// FP32 the packed copy (one 16-byte load plus one 4-byte load).
 template <typename R>
 __device__ __forceinline__ PrimPair<R> load_prim(const sq_slots &sl, long long idx) {
     if constexpr (std::is_same<R, double>::value) {
         const long long NPP = sl.npp_total;
         return PrimPair<R>{__ldg(sl.prim + idx), __ldg(sl.prim + NPP + idx), __ldg(sl.prim + 2 * NPP + idx),
                            __ldg(sl.prim + 3 * NPP + idx), __ldg(sl.prim + 4 * NPP + idx)};
+    } else if constexpr (is_df<R>) {
+        const long long NPP = sl.npp_total;
+        const dfl *pd = reinterpret_cast<const dfl *>(sl.primdf);
+        return PrimPair<R>{df_load(pd + idx), df_load(pd + NPP + idx), df_load(pd + 2 * NPP + idx),
+                           df_load(pd + 3 * NPP + idx), df_load(pd + 4 * NPP + idx)};
     } else {
         const float4 a = __ldg(reinterpret_cast<const float4 *>(sl.prim32v) + 2 * idx);
         return PrimPair<R>{a.x, a.y, a.z, a.w, __ldg(sl.prim32v + 8 * idx + 4)};
@@ -235,6 +252,8 @@ __device__ __forceinline__ void ket_loop(const EriArgs &args, R p, R Px, R Py, R
         R F[L + 1];
         if constexpr (std::is_same<R, double>::value) {
             boys64<L>(T, args.tab64, F);
+        } else if constexpr (is_df<R>) {
+            boys_df<L>(T, reinterpret_cast<const float4 *>(args.tab32 + SQ_BOYS_DF_OFF), F);
         } else if constexpr (BOYS == BOYS_FP64) {
             boys_mixed<L>(T, tb, F);
         } else {
@@ -340,16 +359,20 @@ __device__ __forceinline__ void bra_transform(const R *eb, int sb, R ub,
     }
 }
 
+// acc += x for an FP32 partial sum x (FP64 or double-float accumulator).
+__device__ __forceinline__ void add_f32(double &acc, float x) { acc += f2d_bits(x); }
+__device__ __forceinline__ void add_f32(dfl &acc, float x) { acc = df_add(acc, x); }
+
 // The same contraction of an FP32 W, each block element computed in FP32 and
-// then added into the FP64 accumulator.
-template <int LA, int LB, int LC, int LD>
-__device__ __forceinline__ void bra_transform_f32_into_f64(
+// then added into the FP64 (or double-float) accumulator.
+template <int LA, int LB, int LC, int LD, typename A>
+__device__ __forceinline__ void bra_transform_f32_into(
     const float *eb, int sb, float ub, const float (&W)[LA + LB + 1][LA + LB + 1][LA + LB + 1][ncart(LC) * ncart(LD)],
-    double (&acc)[ncart(LA) * ncart(LB)][ncart(LC) * ncart(LD)]) {
+    A (&acc)[ncart(LA) * ncart(LB)][ncart(LC) * ncart(LD)]) {
     constexpr int NA = ncart(LA), NB = ncart(LB), NCD = ncart(LC) * ncart(LD);
     if constexpr (LA + LB == 0) {
 #pragma unroll
-        for (int y = 0; y < NCD; ++y) acc[0][y] += f2d_bits(ub * W[0][0][0][y]);
+        for (int y = 0; y < NCD; ++y) add_f32(acc[0][y], ub * W[0][0][0][y]);
     } else {
 #pragma unroll
         for (int a = 0; a < NA; ++a)
@@ -373,7 +396,7 @@ __device__ __forceinline__ void bra_transform_f32_into_f64(
                             for (int y = 0; y < NCD; ++y) part[y] = fmaf(e, W[t][u][v][y], part[y]);
                         }
 #pragma unroll
-                for (int y = 0; y < NCD; ++y) acc[a * NB + b][y] += f2d_bits(part[y]);
+                for (int y = 0; y < NCD; ++y) add_f32(acc[a * NB + b][y], part[y]);
             }
     }
 }
@@ -385,7 +408,7 @@ __device__ __forceinline__ void bra_transform_f32_into_f64(
 // the bra transform), the Hermite coefficients of s-s pairs (exactly 1) are
 // neither loaded nor multiplied, and (ss|ss) accumulates with a single FMA.
 //
-// SPLIT (FP64 launches only): primitive-level precision.  Both slots keep
+// SPLIT (FP64 and double-float launches): primitive-level precision.  Both slots keep
 // their primitive pairs in descending primitive Schwarz factor q, so for bra
 // primitive i the ket primitives with q_i q_k >= tau are a prefix [0, K_i),
 // and K_i does not grow with i.  The prefix runs in FP64; the rest, whose
@@ -395,7 +418,8 @@ template <int LA, int LB, int LC, int LD, typename R, int BOYS, bool SPLIT>
 __device__ __forceinline__ void quartet_block(const EriArgs &args, const SlotDesc &bd, const SlotDesc &kd,
                                               const Boys32Blocks &tb,
                                               R (&acc)[ncart(LA) * ncart(LB)][ncart(LC) * ncart(LD)]) {
-    static_assert(!SPLIT || std::is_same<R, double>::value, "primitive-level precision splits FP64 launches");
+    static_assert(!SPLIT || std::is_same<R, double>::value || is_df<R>,
+                  "primitive-level precision splits FP64 and double-float launches");
     constexpr int NAB = ncart(LA) * ncart(LB), NCD = ncart(LC) * ncart(LD);
     constexpr int LAB = LA + LB;
     constexpr int EB = herm_size(LA, LB);
@@ -430,8 +454,8 @@ __device__ __forceinline__ void quartet_block(const EriArgs &args, const SlotDes
                 float W32[LAB + 1][LAB + 1][LAB + 1][NCD];
                 zero_w<LA, LB, LC, LD, float>(W32);
                 ket_loop<LA, LB, LC, LD, float, BOYS_FP64>(args, b4.x, b4.y, b4.z, b4.w, kd, K, nk, tb, W32);
-                bra_transform_f32_into_f64<LA, LB, LC, LD>(sl.herm32 + bd.hbase + (long long)i * EB * sb, sb, ub,
-                                                           W32, acc);
+                bra_transform_f32_into<LA, LB, LC, LD, R>(sl.herm32 + bd.hbase + (long long)i * EB * sb, sb, ub, W32,
+                                                          acc);
             }
         }
     }
@@ -546,6 +570,8 @@ __device__ __forceinline__ void digest_blocks(const R (&acc)[NA * NB][NC * ND], 
     auto to_d = [](R x) -> double {
         if constexpr (std::is_same<R, double>::value)
             return x;
+        else if constexpr (is_df<R>)
+            return df_to_double(x);
         else
             return f2d_bits(x);
     };
@@ -640,6 +666,8 @@ __global__ void __launch_bounds__(128, kMinBlocks(LA + LB + LC + LD)) eri_class_
         const R *D0;
         if constexpr (std::is_same<R, double>::value)
             D0 = args.D;
+        else if constexpr (is_df<R>)
+            D0 = reinterpret_cast<const dfl *>(args.Ddf);
         else
             D0 = args.D32;
         QuartetRows w;
@@ -658,11 +686,11 @@ __global__ void __launch_bounds__(128, kMinBlocks(LA + LB + LC + LD)) eri_class_
         }
 
         // Permutational weight m = 8 / 2^{[a==b] + [c==d] + [P==Q]}; J gets m/2, K gets m/4.
-        double m = 8.0;
-        if ((bd.pairf >> 30) & 1) m *= 0.5;
-        if ((kd.pairf >> 30) & 1) m *= 0.5;
-        if (bd.pairf == kd.pairf) m *= 0.5;  // sub-slots of a pair count as that pair
-        const R wJ = R(0.5 * m), wK = R(0.25 * m);
+        float m = 8.0f;
+        if ((bd.pairf >> 30) & 1) m *= 0.5f;
+        if ((kd.pairf >> 30) & 1) m *= 0.5f;
+        if (bd.pairf == kd.pairf) m *= 0.5f;  // sub-slots of a pair count as that pair
+        const R wJ = R(0.5f * m), wK = R(0.25f * m);
         for (int di = 0; di < nd; ++di) {
             double *Jd = args.Jacc + di * args.dstride, *Kd = args.Kacc + di * args.dstride;
             if constexpr (PREFETCH_D) {
@@ -678,10 +706,22 @@ __global__ void __launch_bounds__(128, kMinBlocks(LA + LB + LC + LD)) eri_class_
 // Host-side launcher table entry for one quartet class.
 typedef cudaError_t (*eri_launcher)(const EriArgs &args, int mode, int precision, cudaStream_t stream);
 
+// Threads per block of a per-thread launch without an explicit shape: 128,
+// or 64 / 32 when the list is too short to give every SM two blocks.  Each
+// thread works through one whole quartet, so a short list of heavy quartets
+// is bound by one thread's latency: spread over more SMs, its warps stop
+// queueing for the same SM's FP64 (or FP32) pipe.
+inline int default_threads(long long nq) {
+    const long long want = 2LL * sm_count();
+    for (int t = 128; t > 32; t >>= 1)
+        if ((nq + t - 1) / t >= want) return t;
+    return 32;
+}
+
 template <int LA, int LB, int LC, int LD>
 cudaError_t launch_eri_class(const EriArgs &args, int mode, int precision, cudaStream_t stream) {
     if (args.nq <= 0) return cudaSuccess;
-    const int threads = args.cfg_threads > 0 ? args.cfg_threads : 128;
+    const int threads = args.cfg_threads > 0 ? args.cfg_threads : default_threads(args.nq);
     long long blocks = (args.nq + threads - 1) / threads;
     // FP64: many blocks (FP64-bound, heavy-first order balances); FP32: about
     // two waves of persistent blocks so the shared Boys table is loaded rarely.
@@ -706,11 +746,31 @@ cudaError_t launch_eri_class_f64(const EriArgs &args, int mode, int precision, c
     (void)mode;
     (void)precision;
     if (args.nq <= 0) return cudaSuccess;
-    const int threads = args.cfg_threads > 0 ? args.cfg_threads : 128;
+    const int threads = args.cfg_threads > 0 ? args.cfg_threads : default_threads(args.nq);
     long long blocks = (args.nq + threads - 1) / threads;
     const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : sm_count() * 16 * 8;
     if (blocks > cap) blocks = cap;
     eri_class_kernel<LA, LB, LC, LD, double, BOYS_FP64, MODE_JK><<<(int)blocks, threads, 0, stream>>>(args);
+    return cudaGetLastError();
+}
+
+// Double-float launcher (SQ_DF64): every quartet of the list in double-float
+// arithmetic on the FP32 pipe, with the primitive quartets below prim_tau in
+// FP32 (prim_tau = 0: none) in the classes with L <= 4.  The heavier classes
+// run whole in double-float: their d pairs have one primitive pair, so the
+// split would move little, and without its FP32 branch the kernels compile in
+// half the time.
+template <int LA, int LB, int LC, int LD>
+cudaError_t launch_eri_class_df(const EriArgs &args, int mode, int precision, cudaStream_t stream) {
+    constexpr bool kSplit = LA + LB + LC + LD <= 4;
+    (void)mode;
+    (void)precision;
+    if (args.nq <= 0) return cudaSuccess;
+    const int threads = args.cfg_threads > 0 ? args.cfg_threads : default_threads(args.nq);
+    long long blocks = (args.nq + threads - 1) / threads;
+    const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : sm_count() * 16 * 8;
+    if (blocks > cap) blocks = cap;
+    eri_class_kernel<LA, LB, LC, LD, dfl, BOYS_FP64, MODE_JK, kSplit><<<(int)blocks, threads, 0, stream>>>(args);
     return cudaGetLastError();
 }
 
@@ -721,7 +781,7 @@ cudaError_t launch_eri_class_f32(const EriArgs &args, int mode, int precision, c
     (void)mode;
     (void)precision;
     if (args.nq <= 0) return cudaSuccess;
-    const int threads = args.cfg_threads > 0 ? args.cfg_threads : 128;
+    const int threads = args.cfg_threads > 0 ? args.cfg_threads : default_threads(args.nq);
     long long blocks = (args.nq + threads - 1) / threads;
     const long long cap = args.cfg_threads > 0 ? args.cfg_blocks : sm_count() * 16;
     if (blocks > cap) blocks = cap;

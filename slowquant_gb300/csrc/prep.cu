@@ -54,6 +54,17 @@ __global__ void boys_taylor_kernel(double *tab64, float *tab32) {
     tab64[SQ_BOYS_TAY64_OFF + idx] = val;
     if (tab32 && j < 4) tab32[SQ_BOYS_TAY32_OFF + mk * 4 + j] = (float)val;
     if (tab32 && j == 4) tab32[SQ_BOYS_TAY32_5_OFF + mk] = (float)val;
+    if (tab32) {
+        // double-float row: c0..c3 as (hi, lo) pairs, c4..c6 as floats, one pad
+        float *row = tab32 + SQ_BOYS_DF_OFF + (long long)mk * 12;
+        const float h = (float)val;
+        if (j < 4) {
+            row[2 * j] = h;
+            row[2 * j + 1] = (float)(val - (double)h);
+        } else {
+            row[4 + j] = j < kBoysTaylor64 ? h : 0.0f;
+        }
+    }
 }
 
 __global__ void boys_eval_kernel(int n_max, const double *z, long long nz, const double *tab, int mode,
@@ -446,6 +457,11 @@ __global__ void slots_fill_kernel(const sq_basis basis, const sq_pairs pairs, sq
             slots.prim[f * NPP + dst] = v;
             if (slots.prim32) slots.prim32[f * NPP + dst] = (float)v;
             if (slots.prim32v) slots.prim32v[8 * dst + f] = (float)v;
+            if (slots.primdf) {
+                const float h = (float)v;
+                slots.primdf[2 * (f * NPP + dst)] = h;
+                slots.primdf[2 * (f * NPP + dst) + 1] = (float)(v - (double)h);
+            }
         }
         if (slots.prim32v) {
             slots.prim32v[8 * dst + 5] = pairs.pq ? (float)pairs.pq[src + kk] : 0.0f;
@@ -457,6 +473,11 @@ __global__ void slots_fill_kernel(const sq_basis basis, const sq_pairs pairs, sq
             const long long d = hb + ((long long)k * E + e) * stride;
             slots.herm[d] = v;
             if (slots.herm32) slots.herm32[d] = (float)v;
+            if (slots.hermdf) {
+                const float h = (float)v;
+                slots.hermdf[2 * d] = h;
+                slots.hermdf[2 * d + 1] = (float)(v - (double)h);
+            }
         }
     }
 }
@@ -495,6 +516,16 @@ __global__ void fock_build_kernel(int nbf, const double *H, const double *Jacc, 
 __global__ void to_float_kernel(long long n, const double *x, float *y) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) y[i] = (float)x[i];
+}
+
+// x as double-float pairs: y[2i] = (float)x[i], y[2i+1] = (float)(x[i] - y[2i]).
+__global__ void to_df_kernel(long long n, const double *x, float2 *y) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const double v = x[i];
+        const float h = (float)v;
+        y[i] = make_float2(h, (float)(v - (double)h));
+    }
 }
 
 }  // namespace sq
@@ -603,6 +634,12 @@ int to_float(long long n, const double *x, float *y, cudaStream_t stream) {
     if (n <= 0) return SQ_OK;
     to_float_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, x, y);
     return check_launch("to_float");
+}
+
+int to_df(long long n, const double *x, float *y, cudaStream_t stream) {
+    if (n <= 0) return SQ_OK;
+    to_df_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, x, reinterpret_cast<float2 *>(y));
+    return check_launch("to_df");
 }
 }  // namespace sq
 

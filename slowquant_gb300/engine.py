@@ -448,6 +448,9 @@ class IntegralEngine:
         self.t_slot_prim32 = torch.empty(max(5 * poff, 1), dtype=torch.float32, device=dev) if self.fp32 else None
         self.t_slot_herm32 = torch.empty(max(hoff, 1), dtype=torch.float32, device=dev) if self.fp32 else None
         self.t_slot_prim32v = torch.empty(max(8 * poff, 1), dtype=torch.float32, device=dev) if self.fp32 else None
+        # double-float copies (hi, lo) for the df64 J/K kernels
+        self.t_slot_primdf = torch.empty(max(10 * poff, 2), dtype=torch.float32, device=dev) if self.fp32 else None
+        self.t_slot_hermdf = torch.empty(max(2 * hoff, 2), dtype=torch.float32, device=dev) if self.fp32 else None
         self.t_slot_desc = torch.empty(max(8 * nslot, 8), dtype=torch.int32, device=dev)
         # primitive Schwarz factors in the pair table's order, copied into the packed FP32 slot data
         self.t_prim_q = torch.tensor(self.prim_q if len(self.prim_q) else np.zeros(1), dtype=torch.float64,
@@ -463,6 +466,7 @@ class IntegralEngine:
         s.prim_src, s.prim_src_off = ptr(self.t_slot_prim_src), ptr(self.t_slot_prim_src_off)
         s.sub = ptr(self.t_slot_sub)
         s.desc, s.mbase, s.prim32v = ptr(self.t_slot_desc), None, ptr(self.t_slot_prim32v)
+        s.primdf, s.hermdf = ptr(self.t_slot_primdf), ptr(self.t_slot_hermdf)
         self._slots = s
         if self.nslot_base:
             # fill the parents' data only: sub-slots point into it
@@ -725,7 +729,8 @@ class IntegralEngine:
     def jk_accumulate(self, D: torch.Tensor, lists, precisions, Jacc=None, Kacc=None, prim_tau: float = 0.0):
         """Run sq_jk for each (quartet list, precision); returns (Jacc, Kacc).
 
-        Precision "fp64_prim" runs sq_jk_prim with bound ``prim_tau``."""
+        Precision "fp64_prim" runs sq_jk_prim with bound ``prim_tau``, "df64_prim"
+        sq_jk_df with that bound and "df64" sq_jk_df with none."""
         Ja, Ka, D32 = self._scratch()
         if Jacc is None:
             Jacc, Kacc = Ja, Ka
@@ -746,6 +751,14 @@ class IntegralEngine:
                 check(self.lib.sq_jk_prim(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs),
                                           ctypes.byref(self.slots), ctypes.byref(qs), ptr(self.tab64), ptr(self.tab32),
                                           ptr(D), ptr(Jacc), ptr(Kacc), float(prim_tau), s.cuda_stream), "sq_jk_prim")
+                continue
+            if prec in ("df64", "df64_prim"):
+                if getattr(self, "_ddf", None) is None:
+                    self._ddf = torch.empty(2 * self.nbf * self.nbf, dtype=torch.float32, device=self.device)
+                tau = float(prim_tau) if prec == "df64_prim" else 0.0
+                check(self.lib.sq_jk_df(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(self.slots),
+                                        ctypes.byref(qs), ptr(self.tab64), ptr(self.tab32), ptr(D), ptr(self._ddf),
+                                        ptr(Jacc), ptr(Kacc), tau, s.cuda_stream), "sq_jk_df")
                 continue
             check(self.lib.sq_jk(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(self.slots),
                                  ctypes.byref(qs), ptr(self.tab64), ptr(self.tab32), ptr(D), ptr(D32), ptr(Jacc),
@@ -770,13 +783,17 @@ class IntegralEngine:
         the large-bound quartets (classes with per-thread kernels);
         "mixed_prim": the "mixed" lists, with the large-bound quartets' primitive
         quartets of bound q_ij q_kl < fp32_threshold run in FP32 inside the FP64
-        launch (sq_jk_prim).
+        launch (sq_jk_prim); "df64": every quartet in double-float arithmetic on
+        the FP32 pipe (sq_jk_df, classes (ss|ss)-(dd|ds); the others FP64);
+        "mixed_df": "mixed_prim" with double-float in place of FP64.
         """
         if precision == "fp64":
             return [self.quartets(threshold)], ["fp64"]
-        if precision == "mixed_prim":
+        if precision == "df64":
+            return [self.quartets(threshold)], ["df64"]
+        if precision in ("mixed_prim", "mixed_df"):
             q64, q32 = self.quartets(threshold, fp32_threshold)
-            return [q64, q32], ["fp64_prim", "fp32"]
+            return [q64, q32], ["fp64_prim" if precision == "mixed_prim" else "df64_prim", "fp32"]
         if precision not in ("mixed", "mixed_boys32", "mixed_chunk"):
             raise ValueError(f"unknown precision {precision!r}")
         q64, q32 = self.quartets(threshold, fp32_threshold, chunks=precision == "mixed_chunk")
@@ -786,8 +803,8 @@ class IntegralEngine:
                  fp32_threshold: float = 1e-4):
         """J_i, K_i (symmetrised, [nd, nbf, nbf]) for a stack of densities Ds [nd, nbf, nbf],
         with each quartet's integrals evaluated once for all of them (sq_jk_multi)."""
-        if precision == "mixed_prim":
-            raise ValueError("precision 'mixed_prim' serves one density per call (use 'mixed' for several)")
+        if precision in ("mixed_prim", "mixed_df", "df64"):
+            raise ValueError(f"precision {precision!r} serves one density per call (use 'mixed' for several)")
         lists, precs = self._lists_for(precision, threshold, fp32_threshold)
         Ds = Ds.to(device=self.device, dtype=torch.float64).contiguous()
         nd = Ds.shape[0]
@@ -811,7 +828,8 @@ class IntegralEngine:
 
         precision: "fp64" (every quartet FP64), "mixed" (bound < fp32_threshold
         in FP32 with FP64 Boys), "mixed_boys32" (those quartets fully FP32),
-        "mixed_chunk" and "mixed_prim" (the same test at finer grain, see _lists_for).
+        "mixed_chunk" and "mixed_prim" (the same test at finer grain), "df64" and
+        "mixed_df" (double-float arithmetic in place of FP64), see _lists_for.
         """
         lists, precs = self._lists_for(precision, threshold, fp32_threshold)
         Jacc, Kacc = self.jk_accumulate(D, lists, precs, prim_tau=fp32_threshold)

@@ -84,11 +84,14 @@ class DirectJK:
     """Integral-direct J/K callable for run_hartree_fock.
 
     precision: "fp64", "mixed" (quartets with Schwarz bound < fp32_threshold in
-    FP32 with FP64 Boys recursion), "mixed_boys32", "mixed_chunk" or
+    FP32 with FP64 Boys recursion), "mixed_boys32", "mixed_chunk",
     "mixed_prim" (the bound test per primitive quartet inside the large-bound
-    quartets, see IntegralEngine._lists_for).  In mixed modes the SCF
-    switches to FP64 once the DIIS error max|FDS - SDF| drops below
-    ``fp64_tail_diis_error`` (call ``switch_to_fp64``).
+    quartets), "df64" (double-float arithmetic in place of FP64) or
+    "mixed_df" ("mixed_prim" with double-float in place of FP64), see
+    IntegralEngine._lists_for.  In mixed modes the SCF switches to the
+    accurate arithmetic (FP64; double-float for "mixed_df") once the DIIS
+    error max|FDS - SDF| drops below ``fp64_tail_diis_error`` (call
+    ``switch_to_fp64``).
     """
 
     def __init__(self, engine, threshold: float = 1e-12, precision: str = "fp64", fp32_threshold: float = 1e-4,
@@ -102,10 +105,10 @@ class DirectJK:
 
     @property
     def mixed(self) -> bool:
-        return self.precision != "fp64"
+        return self.precision not in ("fp64", "df64")
 
     def switch_to_fp64(self) -> None:
-        self.precision = "fp64"
+        self.precision = "df64" if self.precision == "mixed_df" else "fp64"
 
     def __call__(self, D: torch.Tensor):
         self.builds.append(self.precision)
@@ -213,8 +216,8 @@ class _HartreeFock:
 
     Extra knobs beyond the reference: ``direct_jk`` (default True: integral-
     direct Fock builds instead of the stored ERI tensor), ``precision``
-    ("fp64" | "mixed" | "mixed_boys32"), ``fp32_schwarz_threshold``,
-    ``fp64_tail_diis_error``.
+    (a DirectJK precision: "fp64", "mixed", "mixed_prim", "df64", "mixed_df",
+    ...), ``fp32_schwarz_threshold``, ``fp64_tail_diis_error``.
     """
 
     def __init__(self, molecule_obj, integral_obj) -> None:

@@ -243,7 +243,8 @@ def test_header_constants_match_python_bindings():
         if n in d:
             assert getattr(_lib, n) == d[n], n
     for n in ("SQ_MAX_L", "SQ_MAX_QCLASS", "SQ_MAX_L_GRAD", "SQ_BOYS_TAB64_SIZE", "SQ_BOYS_TAB32_SIZE",
-              "SQ_BOYS_HI64_OFF", "SQ_ERR_UNSUPPORTED", "SQ_OPT_JK_STREAMS"):
+              "SQ_BOYS_HI64_OFF", "SQ_BOYS_TAY64_OFF", "SQ_BOYS_DF_OFF", "SQ_DF64", "SQ_ERR_UNSUPPORTED",
+              "SQ_OPT_JK_STREAMS"):
         assert n in d and getattr(_lib, n) == d[n], n
     # 10 pair classes (la >= lb, l <= 3) -> 55 quartet classes; the grids fit the orders used
     npc = (d["SQ_MAX_L"] + 1) * (d["SQ_MAX_L"] + 2) // 2
@@ -333,6 +334,7 @@ def test_abi_refuses_bad_arguments_before_touching_the_device():
         assert L.sq_jk(None, None, None, None, None, None, None, None, None, None, 0, None) == _lib.SQ_ERR_ARG
         assert b"NULL" in L.sq_last_error()
         assert L.sq_grad_2e(None, None, None, None, None, None, None, None) == _lib.SQ_ERR_ARG
+        assert L.sq_jk_df(None, None, None, None, None, None, None, None, None, None, 0.0, None) == _lib.SQ_ERR_ARG
         assert L.sq_batched_eigh(1, p, p, 129, p, p, p, p, 1e-12, 10, None, None) == _lib.SQ_ERR_ARG
         assert b"dimension" in L.sq_last_error()
     finally:
