@@ -33,7 +33,18 @@ WATERS, BOX, SEED, BASIS = 16, 11.0, 16, "cc-pvdz"
 BOXES = {16: 11.0, 8: 9.0}
 # Cartesian basis functions per water and the basis's name as printed
 BASES = {"cc-pvdz": (25, "cc-pVDZ"), "cc-pvtz": (65, "cc-pVTZ")}
-SCREEN, FP32_THR = 1e-12, 1e-4
+SCREEN, FP32_THR = 1e-12, 1e-3
+# precision mode of the headline build, and the launch precision of its large-bound list
+HEADLINE = "mixed_df"
+ACCURATE_LIST = {"mixed": "fp64", "mixed_prim": "fp64_prim", "mixed_df": "df64_prim"}
+HEADLINE_TEXT = {
+    "mixed": "mixed (quartets with Schwarz bound below {tau:g} in FP32 with the FP64 Boys recursion; FP64 above)",
+    "mixed_prim": "mixed_prim (FP64 for the large-bound quartets, their primitive quartets below {tau:g} in FP32; "
+                  "FP32 quartets below the bound)",
+    "mixed_df": "mixed_df (double-float arithmetic on the FP32 pipe, about 46 bits, for the large-bound quartets of "
+                "the classes where it is faster, FP64 for the others; their primitive quartets below {tau:g} and "
+                "the quartets below {tau:g} in FP32)",
+}
 
 
 def workload_geometry() -> str:
@@ -63,7 +74,7 @@ def config(extra=None) -> dict:
         "basis": f"{label} (Cartesian, {nbf_w * WATERS} bf)",
         "schwarz_threshold": SCREEN,
         "fp32_schwarz_threshold": FP32_THR,
-        "precision": "mixed (FP32 quartets below bound 1e-4, FP64 Boys recursion; FP64 above)",
+        "precision": HEADLINE_TEXT[HEADLINE].format(tau=FP32_THR),
         "step": "one Fock build F = H + J - K/2 from a converged-SCF density",
         "l2": "flushed between timed steps (512 MB write); quartet list > L2",
         "parallelism": "replicas only",
@@ -135,7 +146,7 @@ def fma_peak(lib, torch, precision: int) -> float:
     from slowquant_gb300 import _lib
 
     sms = torch.cuda.get_device_properties(0).multi_processor_count
-    blocks, iters = sms * 8, (20000 if precision == _lib.SQ_FP64 else 400000)
+    blocks, iters = sms * 8, {_lib.SQ_FP64: 20000, _lib.SQ_DF64: 30000}.get(precision, 400000)
     out = torch.empty(blocks * 256, dtype=torch.float64, device="cuda")
     s = _lib.stream_handle()
     _lib.check(lib.sq_fma_probe(precision, blocks, 100, out.data_ptr(), s), "sq_fma_probe")
@@ -349,7 +360,7 @@ def gpu_arm(args) -> None:
     t0 = time.time()
     E64, C64, F64, D64 = run_hartree_fock(S, T, V, jk64, ne, log, 1e-9, 1e-9, 100, True)
     scf64_s = time.time() - t0
-    jkm = DirectJK(eng, SCREEN, "mixed", FP32_THR, 1e-5)
+    jkm = DirectJK(eng, SCREEN, HEADLINE, FP32_THR, 1e-5)
     t0 = time.time()
     Em, _, _, _ = run_hartree_fock(S, T, V, jkm, ne, log, 1e-9, 1e-9, 100, True)
     scfm_s = time.time() - t0
@@ -362,7 +373,7 @@ def gpu_arm(args) -> None:
         flush_buf.zero_()
 
     def step_mixed():
-        eng.fock(H, D, SCREEN, "mixed", FP32_THR)
+        eng.fock(H, D, SCREEN, HEADLINE, FP32_THR)
 
     def step_fp64():
         eng.fock(H, D, SCREEN, "fp64")
@@ -400,7 +411,7 @@ def gpu_arm(args) -> None:
 
     def step_e2e():
         Dd = D_host.to("cuda", non_blocking=True)
-        F = eng.fock(H, Dd, SCREEN, "mixed", FP32_THR)
+        F = eng.fock(H, Dd, SCREEN, HEADLINE, FP32_THR)
         F_host.copy_(F, non_blocking=True)
 
     for _ in range(2):
@@ -428,7 +439,7 @@ def gpu_arm(args) -> None:
 
     # primitive-chunk granularity of the same precision test (beside the headline)
     chunk_modes = []
-    for tau in (FP32_THR, 1e-3, 1e-2):
+    for tau in (1e-4, 1e-3, 1e-2):
         eng.fock(H, D, SCREEN, "mixed_chunk", tau)
         ms_c = float(np.median(time_events(torch, lambda: eng.fock(H, D, SCREEN, "mixed_chunk", tau), 5, flush)))
         Fc = eng.fock(H, D, SCREEN, "mixed_chunk", tau)
@@ -516,30 +527,36 @@ def gpu_arm(args) -> None:
 
     # the two halves of the mixed build, each timed alone (all its classes, stream pool)
     ms_part = {}
-    for name, lst, prec in (("fp64_list", q64, "fp64"), ("fp32_list", q32, "fp32")):
-        eng.jk_accumulate(D, [lst], [prec])
-        ms_part[name] = float(np.median(time_events(torch, lambda: eng.jk_accumulate(D, [lst], [prec]), 5, flush)))
+    for name, lst, prec in (("fp64_list", q64, ACCURATE_LIST[HEADLINE]), ("fp32_list", q32, "fp32")):
+        eng.jk_accumulate(D, [lst], [prec], prim_tau=FP32_THR)
+        ms_part[name] = float(np.median(time_events(
+            torch, lambda: eng.jk_accumulate(D, [lst], [prec], prim_tau=FP32_THR), 5, flush)))
 
     # roofline of the dominant kernel (per-class launches timed alone)
     peak64 = fma_peak(lib, torch, _lib.SQ_FP64)
     peak32 = fma_peak(lib, torch, _lib.SQ_FP32)
+    peakdf = fma_peak(lib, torch, _lib.SQ_DF64)
     work64 = class_work(eng, q64)
     work32 = class_work(eng, q32, "fp32")
     work_all = class_work(eng, q_all)
     rows = []
-    for lst, prec, work in ((q64, "fp64", work64), (q32, "fp32", work32)):
+    for lst, prec, work in ((q64, ACCURATE_LIST[HEADLINE], work64), (q32, "fp32", work32)):
         for c, w in work.items():
             off = np.zeros(_lib.SQ_MAX_QCLASS + 1, dtype=np.int64)
             off[c + 1:] = w["list_entries"]
             sub = QuartetList(lst.pairs[lst.class_off[c]:lst.class_off[c + 1]], off)
-            eng.jk_accumulate(D, [sub], [prec])
-            t = float(np.median(time_events(torch, lambda: eng.jk_accumulate(D, [sub], [prec]), 3, flush)))
-            rows.append({"class": w["class"], "precision": prec, "ms": t, "flops": w["flops"],
+            eng.jk_accumulate(D, [sub], [prec], prim_tau=FP32_THR)
+            t = float(np.median(time_events(
+                torch, lambda: eng.jk_accumulate(D, [sub], [prec], prim_tau=FP32_THR), 3, flush)))
+            # the arithmetic the launch ran in (the library's per-class double-float policy)
+            ran = prec if prec in ("fp64", "fp32") else (
+                "df64" if prec == "df64_prim" and eng.df_class(c, w["list_entries"]) else "fp64")
+            rows.append({"class": w["class"], "precision": ran, "ms": t, "flops": w["flops"],
                          "quartets": w["quartets"]})
     rows.sort(key=lambda r: -r["ms"])
     dom = rows[0]
     # The J/K launch also zeroes two nbf^2 accumulators (negligible at 400 bf).
-    peak = peak64 if dom["precision"] == "fp64" else peak32
+    peak = {"fp64": peak64, "fp32": peak32, "df64": peakdf}[dom["precision"]]
     achieved = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
     fl64 = sum(w["flops"] for w in work_all.values())
     launches = sum(1 for c in range(_lib.SQ_MAX_QCLASS) if q64.class_off[c + 1] > q64.class_off[c]) + sum(
@@ -589,10 +606,12 @@ def gpu_arm(args) -> None:
     line = {
         "metric": METRIC, "value": value, "unit": "quartets/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64+f32 (mixed)", "data": "synthetic",
+        "vs_baseline": None, "dtype": {"mixed_df": "df64+f64+f32 (mixed)"}.get(HEADLINE, "f64+f32 (mixed)"),
+        "data": "synthetic",
         "config": config({"nbf": eng.nbf, "surviving_quartets": nq, "fp64_quartets": n64_unique,
                           "fp32_quartets": n32_unique, "list_entries_after_split": q_all.nquartet}),
-        "fock_build_ms": {"mixed": ms_step, "fp64": ms64, "speedup_mixed_vs_fp64": ms64 / ms_step,
+        "fock_build_ms": {"mixed": ms_step, "mixed_precision_mode": HEADLINE, "fp64": ms64,
+                          "speedup_mixed_vs_fp64": ms64 / ms_step,
                           "mixed_fp64_list_alone": ms_part["fp64_list"], "mixed_fp32_list_alone": ms_part["fp32_list"]},
         "quartets_per_s": {"mixed": nq / (ms_step * 1e-3), "fp64": nq / (ms64 * 1e-3)},
         "energy": {"E_hf_fp64": E64, "E_hf_mixed": Em, "abs_dE_mixed_vs_fp64": abs(Em - E64),
@@ -606,11 +625,12 @@ def gpu_arm(args) -> None:
         "e2e": {"value": world * nq / (e2e_ms * 1e-3), "unit": "quartets/s",
                 "h2d_bytes_per_step": int(D.numel() * 8), "d2h_bytes_per_step": int(D.numel() * 8),
                 "ms_per_step": e2e_ms},
-        "roofline": {"bound": "fp64" if dom["precision"] == "fp64" else "fp32",
+        "roofline": {"bound": {"fp64": "fp64", "fp32": "fp32", "df64": "fp32 (double-float)"}[dom["precision"]],
                      "kernel": f"J/K class ({dom['class'][0]}{dom['class'][1]}|{dom['class'][2]}{dom['class'][3]}) "
                                f"{dom['precision']}",
                      "achieved": achieved, "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / (peak / 1e12),
-                     "peak_source": "measured by sq_fma_probe (FMA loop) in this run",
+                     "peak_source": "measured by sq_fma_probe (FMA loop, in the kernel's arithmetic) in this run",
+                     "peaks_tflops": {"fp64": peak64 / 1e12, "df64": peakdf / 1e12, "fp32": peak32 / 1e12},
                      "traffic": None, "flops_per_launch": dom["flops"], "ms_per_launch": dom["ms"]},
         "roofline_fp64_build": {"flops": fl64, "ms": ms64, "achieved_tflops": fl64 / (ms64 * 1e-3) / 1e12,
                                 "peak_tflops": peak64 / 1e12, "frac": fl64 / (ms64 * 1e-3) / peak64},
@@ -788,6 +808,7 @@ def gradient_arm(args) -> None:
 
 
 def main() -> None:
+    global WATERS, SEED, BASIS, HEADLINE, FP32_THR
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -811,10 +832,14 @@ def main() -> None:
                     help="bounds of the primitive-level precision mode reported beside the headline (empty: skip)")
     ap.add_argument("--no-df", dest="df", action="store_false",
                     help="skip the double-float (df64, mixed_df) measurements")
+    ap.add_argument("--precision", default=HEADLINE, choices=sorted(ACCURATE_LIST),
+                    help="precision mode of the headline mixed build")
+    ap.add_argument("--fp32-threshold", type=float, default=FP32_THR,
+                    help="bound below which quartets (and, in mixed_prim / mixed_df, primitive quartets) run in FP32")
     args = ap.parse_args()
-    global WATERS, SEED, BASIS
     WATERS = SEED = args.waters
     BASIS = args.basis
+    HEADLINE, FP32_THR = args.precision, args.fp32_threshold
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -218,12 +218,16 @@ const char *sq_last_error(void);
  * ((ss|ss), (ps|ss), (ps|ps), (pp|ss), (pp|ps), (ds|ss), (ds|ps), (dp|ss))
  * one quartet per thread, 0 one quartet per warp like the other classes. */
 #define SQ_OPT_GRAD_THREAD 4
-/* SQ_OPT_DF_CLASSES: bit mask over quartet classes 0-18; a set bit runs the
- * class's SQ_DF64 launches (sq_jk_df) on its double-float kernel, a clear bit
- * as in sq_jk_prim (FP64 with the primitive split where the class has it).
- * Default: the classes where double-float measured faster, SQ_DF_CLASSES_DEFAULT. */
+/* SQ_OPT_DF_CLASSES: which classes of an SQ_DF64 launch (sq_jk_df) run on
+ * their double-float kernel; the others run as in sq_jk_prim (FP64, with the
+ * primitive split where the class has it).  -1 (default): the measured
+ * policy -- always for (ss|ss), (ps|ss), (ps|ps), (pp|ss), (ds|ss), (ds|ps),
+ * (dp|ss), (dd|ss), (dd|ps); for (pp|ps), (pp|pp), (ds|pp), (ds|ds), (dp|ps)
+ * when the launch holds at least 512 quartets per SM; never for (dp|pp),
+ * (dp|ds), (dp|dp), (dd|pp), (dd|ds), whose double-float kernels spill more
+ * than their FP64 ones.  A mask >= 0 over classes 0-18 selects exactly the
+ * set bits, whatever the launch length. */
 #define SQ_OPT_DF_CLASSES 5
-#define SQ_DF_CLASSES_DEFAULT 0x7FFFFLL
 int sq_set_option(int key, long long value);
 long long sq_get_option(int key);
 
@@ -337,6 +341,11 @@ int sq_jk_df(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots
              const double *table64, const float *table32, const double *D, float *Ddf, double *Jacc, double *Kacc,
              double prim_tau, void *stream);
 
+/* 1 when an SQ_DF64 launch of quartet class qclass holding nquartets list
+ * entries runs on the class's double-float kernel (option SQ_OPT_DF_CLASSES),
+ * else 0.  Host-only query. */
+int sq_df_class(int qclass, long long nquartets);
+
 /* J/K build for callers that cannot allocate device memory.  No counterpart
  * in the reference (it has no device code).  Same arguments and results as
  * sq_jk, minus D32: the FP32 density scratch that FP32 launches need lives in
@@ -423,9 +432,11 @@ int sq_batched_eigh(int nmat, const long long *offsets, const int *dims, int max
 
 /* Arithmetic-pipe probe (no reference counterpart): blocks x 256 threads each
  * run `iters` iterations of 8 independent FMA chains in FP64 (precision
- * SQ_FP64) or FP32 (otherwise), i.e. 16 * iters * 256 * blocks FLOPs; out
- * holds blocks*256 elements of that type.  Timing it gives the measured FMA
- * peak used as the roofline denominator of the FP64/FP32-pipe-bound kernels. */
+ * SQ_FP64), double-float (SQ_DF64: float pairs, csrc/df64.cuh) or FP32
+ * (otherwise), i.e. 16 * iters * 256 * blocks FLOPs; out holds blocks*256
+ * elements of that type (8 bytes for SQ_DF64).  Timing it gives the measured
+ * FMA peak used as the roofline denominator of the FP64-, double-float- and
+ * FP32-bound kernels. */
 int sq_fma_probe(int precision, int blocks, int iters, void *out, void *stream);
 
 #ifdef __cplusplus

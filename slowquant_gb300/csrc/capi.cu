@@ -106,8 +106,19 @@ static int g_generic_min_l = 5;
 // Bit c set: the FP64 J/K launches of class c run on its kLaunchersF64 kernel,
 // else on the warp kernel (option SQ_OPT_FP64_UNROLLED_HIGH).
 static long long g_fp64_unrolled_high = 0x7FLL << 12;  // classes 12-18
-// Bit c set: SQ_DF64 launches of class c run on its double-float kernel (option SQ_OPT_DF_CLASSES).
-static long long g_df_classes = SQ_DF_CLASSES_DEFAULT;
+// Classes of SQ_DF64 launches on the double-float kernels (option SQ_OPT_DF_CLASSES):
+// -1 the measured policy kDfPolicy, else a bit mask.
+static long long g_df_classes = -1;
+// Per class, measured on the (H2O)16 cc-pVDZ lists against the FP64 kernels:
+// 2 double-float is faster at any launch length; 1 only on long launches
+// (throughput-bound; a short launch is bound by one thread's latency, and a
+// double-float operation is a longer dependent chain than one FP64 FMA);
+// 0 never (the double-float kernel spills more than the FP64 one).
+static const signed char kDfPolicy[SQ_MAX_QCLASS] = {2, 2, 2, 2, 1, 1, 2, 2, 1, 1, 2, 1, 0, 0, 0, 2, 2, 0, 0};
+static bool df_class(int c, long long nq) {
+    if (g_df_classes >= 0) return (g_df_classes >> c) & 1;
+    return kDfPolicy[c] == 2 || (kDfPolicy[c] == 1 && nq >= 512LL * sm_count());
+}
 // Per-thread gradient kernels for the light classes (option SQ_OPT_GRAD_THREAD).
 static int g_grad_thread = 1;
 int grad_thread_enabled() { return g_grad_thread; }
@@ -202,7 +213,7 @@ static cudaError_t launch_class(EriArgs &args, const sq_quartets *qs, int c, int
     // SQ_DF64 runs on the double-float kernels where a class has one, else as
     // SQ_FP64_PRIM (which keeps the per-thread f classes' split)
     if (mode == MODE_JK && precision == SQ_DF64) {
-        if (kLaunchersDF[c] != nullptr && g_generic_min_l > 0 && ((g_df_classes >> c) & 1))
+        if (kLaunchersDF[c] != nullptr && g_generic_min_l > 0 && df_class(c, args.nq))
             return kLaunchersDF[c](args, mode, precision, stream);
         return launch_class(args, qs, c, mode, SQ_FP64_PRIM, stream);
     }
@@ -287,7 +298,7 @@ extern "C" int sq_set_option(int key, long long value) {
         return SQ_OK;
     }
     if (key == SQ_OPT_DF_CLASSES) {
-        if (value < 0 || value >= (1LL << SQ_MAX_QCLASS))
+        if (value < -1 || value >= (1LL << SQ_MAX_QCLASS))
             return set_error(SQ_ERR_ARG, "sq_set_option: class mask out of range");
         g_df_classes = value;
         return SQ_OK;
@@ -430,6 +441,11 @@ extern "C" int sq_jk_df(const sq_basis *basis, const sq_pairs *pairs, const sq_s
                         float *Ddf, double *Jacc, double *Kacc, double prim_tau, void *stream) {
     return jk_common("sq_jk_df", basis, pairs, slots, quartets, table64, table32, 1, D, nullptr, Jacc, Kacc,
                      SQ_DF64, stream, true, (float)prim_tau, Ddf);
+}
+
+extern "C" int sq_df_class(int qclass, long long nquartets) {
+    if (qclass < 0 || qclass >= SQ_MAX_QCLASS) return 0;
+    return kLaunchersDF[qclass] != nullptr && g_generic_min_l > 0 && df_class(qclass, nquartets);
 }
 
 extern "C" int sq_jk_multi(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slots,

@@ -660,12 +660,31 @@ __global__ void fma_probe_kernel(T *out, int iters, T a, T b) {
     for (int k = 0; k < 8; ++k) s += x[k];
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
+
+// The same chains in double-float arithmetic (csrc/df64.cuh): one fma is two
+// FP64-model FLOPs carried out by about fifteen FP32 instructions.
+__global__ void fma_probe_df_kernel(float2 *out, int iters, dfl a, dfl b) {
+    dfl x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = dfl((float)(threadIdx.x + k));
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+    }
+    dfl s(0.0f);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s = s + x[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = make_float2(s.hi, s.lo);
+}
 }  // namespace sq
 
 extern "C" int sq_fma_probe(int precision, int blocks, int iters, void *out, void *stream) {
     if (blocks <= 0 || iters <= 0 || !out) return set_error(SQ_ERR_ARG, "sq_fma_probe: bad argument");
     if (precision == SQ_FP64)
         sq::fma_probe_kernel<double><<<blocks, 256, 0, (cudaStream_t)stream>>>((double *)out, iters, 1.0000001, 1e-9);
+    else if (precision == SQ_DF64)
+        sq::fma_probe_df_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>((float2 *)out, iters, sq::dfl(1.0000001),
+                                                                          sq::dfl(1e-9));
     else
         sq::fma_probe_kernel<float><<<blocks, 256, 0, (cudaStream_t)stream>>>((float *)out, iters, 1.0000001f, 1e-9f);
     return check_launch("sq_fma_probe");

@@ -50,6 +50,13 @@ PRIM_SCREEN = 1e-17
 SPLIT_TARGET = 512
 # primitive pairs per chunk (at least) in the per-chunk precision mode
 CHUNK_MIN = 2
+# heavy per-thread classes, (dp|pp) to (dd|ds): a short list of them is bound by
+# one thread's serial, spilled quartet; below KET_SPLIT_PER_SM entries per SM
+# (one register file of 255-register threads) their quartets are cut into ket
+# sub-slot chunks (at most KET_SPLIT_MAX), which multiplies the threads in flight
+KET_SPLIT_CLASSES = frozenset(range(12, 19))
+KET_SPLIT_PER_SM = 256
+KET_SPLIT_MAX = 8
 # f-shell classes with per-thread J/K kernels in every precision: (fs|ss), (fs|ps), (fp|ss)
 F_PER_THREAD = frozenset({21, 22, 28})
 _W_SSSS = flops.flops_per_primitive_quartet(0, 0, 0, 0)
@@ -508,10 +515,55 @@ class IntegralEngine:
             out = self._chunk_lists(lists, ket_list, float(fp32_threshold), s64)
         else:
             out = [self._expand(t, ket_list, split_sets[li]) for li, t in enumerate(lists)]
+        if split:
+            out = [self._ket_split(ql, split_sets[li] & KET_SPLIT_CLASSES) for li, ql in enumerate(out)]
         res = out[0] if len(out) == 1 else (out[0], out[1])
         if own:
             self._quartet_cache[key] = res
         return res
+
+    def _ket_split(self, ql: QuartetList, classes) -> QuartetList:
+        """Cut the ket of every quartet of a short heavy-class segment into sub-slot chunks.
+
+        A class segment of n < KET_SPLIT_PER_SM * SMs entries asks for S = the
+        power of two (at most KET_SPLIT_MAX) that brings it to that size; each
+        entry (bra, ket) with a whole ket slot becomes (bra, chunk j of S') for
+        the largest S' <= S its ket has chunks for.  J and K are linear in the
+        ket's primitive pairs, so the partial quartets add up to the whole."""
+        target = KET_SPLIT_PER_SM * torch.cuda.get_device_properties(self.device).multi_processor_count
+        counts = ql.class_counts()
+        todo = [c for c in sorted(classes) if 0 < counts[c] < target]
+        if not todo or not self.sub_first:
+            return ql
+        host = ql.pairs[: ql.nquartet].cpu().numpy()
+        parts, off = [], np.zeros_like(ql.class_off)
+        for c in range(_lib.SQ_MAX_QCLASS):
+            seg = host[ql.class_off[c]:ql.class_off[c + 1]]
+            if c in todo:
+                want = 1
+                while want < KET_SPLIT_MAX and len(seg) * want < target:
+                    want *= 2
+                ket = seg[:, 1].astype(np.int64)
+                whole = ket < self.nslot_base
+                S = np.ones(len(seg), np.int64)
+                first = np.full(len(seg), -1, np.int64)
+                for s in sorted(self.sub_first):
+                    if s > want:
+                        break
+                    f = np.full(len(seg), -1, np.int64)
+                    f[whole] = self.sub_first[s][ket[whole]]
+                    ok = f >= 0
+                    S[ok] = s
+                    first[ok] = f[ok]
+                rep = np.repeat(np.arange(len(seg)), S)
+                j = np.arange(len(rep)) - np.repeat(np.cumsum(S) - S, S)
+                newket = np.where(np.repeat(S, S) > 1, np.repeat(first, S) + j, np.repeat(ket, S))
+                seg = np.stack([seg[rep, 0], newket.astype(np.int32)], axis=1)
+            parts.append(seg)
+            off[c + 1] = off[c] + len(seg)
+        allp = np.concatenate(parts).astype(np.int32) if int(off[-1]) else np.zeros((0, 2), np.int32)
+        t = torch.tensor(allp, dtype=torch.int32, device=self.device).reshape(-1, 2).contiguous()
+        return QuartetList(t, off)
 
     def _split_classes(self):
         """(FP64, FP32) sets of the classes whose J/K quartets may be split into
@@ -766,6 +818,10 @@ class IntegralEngine:
         for s in side:
             main.wait_stream(s)
         return Jacc, Kacc
+
+    def df_class(self, qclass: int, nquartets: int) -> bool:
+        """True when a "df64"/"df64_prim" launch of this class and length runs in double-float (sq_df_class)."""
+        return bool(self.lib.sq_df_class(int(qclass), int(nquartets)))
 
     def _side_streams(self, n: int):
         if not hasattr(self, "_sides"):

@@ -302,3 +302,27 @@ def test_chunk_lists_partition_exactly_in_fp64():
         K = (0.5 * (Ka + Ka.T)).cpu().numpy()
         np.testing.assert_allclose(J, J0, atol=1e-11)
         np.testing.assert_allclose(K, K0, atol=1e-11)
+
+
+def test_ket_split_lists_give_the_same_jk(monkeypatch):
+    """Short heavy-class segments cut into ket sub-slot chunks: the same J and K, more list entries."""
+    import torch
+
+    from slowquant_gb300 import engine, systems
+
+    geom = systems.water_cluster(3, 6.0, seed=3)
+    eng = _engine(geom, "cc-pvdz", "angstrom")
+    D = torch.tensor(_random_density(eng.nbf, 7), dtype=torch.float64, device="cuda")
+    res = {}
+    for per_sm in (0, engine.KET_SPLIT_PER_SM):
+        monkeypatch.setattr(engine, "KET_SPLIT_PER_SM", per_sm)
+        eng._quartet_cache.clear()
+        ql = eng.quartets(1e-12)
+        res[per_sm] = (ql.class_counts(), [x.cpu().numpy() for x in eng.jk(D, 1e-12, "fp64")],
+                       [x.cpu().numpy() for x in eng.jk(D, 1e-12, "mixed_prim", 1e-3)])
+    (c0, jk0, jp0), (c1, jk1, jp1) = res[0], res[engine.KET_SPLIT_PER_SM]
+    assert sum(c1[12:19]) > sum(c0[12:19]) and (c1[:12] == c0[:12]).all()
+    for a, b in zip(jk0, jk1):
+        np.testing.assert_allclose(b, a, atol=1e-12)
+    for a, b in zip(jp0, jp1):  # the FP32 parts are summed in other groupings: FP32 rounding of terms < 1e-3
+        np.testing.assert_allclose(b, a, atol=1e-8)

@@ -310,10 +310,13 @@ def test_abi_refuses_bad_arguments_before_touching_the_device():
         build.build()
     L = _lib.lib()
     defaults = {k: L.sq_get_option(k) for k in (_lib.SQ_OPT_GENERIC_MIN_L, _lib.SQ_OPT_JK_STREAMS,
-                                                _lib.SQ_OPT_FP64_UNROLLED_HIGH, _lib.SQ_OPT_GRAD_THREAD)}
+                                                _lib.SQ_OPT_FP64_UNROLLED_HIGH, _lib.SQ_OPT_GRAD_THREAD,
+                                                _lib.SQ_OPT_DF_CLASSES)}
     try:
         assert defaults[_lib.SQ_OPT_JK_STREAMS] == 8 and defaults[_lib.SQ_OPT_GENERIC_MIN_L] == 5
         assert defaults[_lib.SQ_OPT_FP64_UNROLLED_HIGH] == 0x7F << 12
+        assert defaults[_lib.SQ_OPT_DF_CLASSES] == -1  # the measured per-class policy
+        assert L.sq_set_option(_lib.SQ_OPT_DF_CLASSES, -2) == _lib.SQ_ERR_ARG
         assert L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, 0) == _lib.SQ_ERR_ARG
         assert L.sq_set_option(_lib.SQ_OPT_JK_STREAMS, 17) == _lib.SQ_ERR_ARG
         assert L.sq_set_option(_lib.SQ_OPT_FP64_UNROLLED_HIGH, 1 << _lib.SQ_MAX_QCLASS) == _lib.SQ_ERR_ARG
