@@ -52,10 +52,13 @@ SPLIT_TARGET = 512
 CHUNK_MIN = 2
 # heavy per-thread classes, (dp|pp) to (dd|ds): a short list of them is bound by
 # one thread's serial, spilled quartet; below KET_SPLIT_PER_SM entries per SM
-# (one register file of 255-register threads) their quartets are cut into ket
-# sub-slot chunks (at most KET_SPLIT_MAX), which multiplies the threads in flight
+# their quartets can be cut into ket sub-slot chunks (at most KET_SPLIT_MAX),
+# which multiplies the threads in flight.  Off (0) by default: on (H2O)16
+# cc-pVDZ, 256 per SM halved those launches timed alone (0.77 -> 0.42 ms for
+# (dp|pp)) but the concurrent builds took longer (mixed_df 6.09 -> 6.40 ms),
+# because the extra digestion work competes with the other classes' launches.
 KET_SPLIT_CLASSES = frozenset(range(12, 19))
-KET_SPLIT_PER_SM = 256
+KET_SPLIT_PER_SM = 0
 KET_SPLIT_MAX = 8
 # f-shell classes with per-thread J/K kernels in every precision: (fs|ss), (fs|ps), (fp|ss)
 F_PER_THREAD = frozenset({21, 22, 28})

@@ -314,13 +314,13 @@ def test_ket_split_lists_give_the_same_jk(monkeypatch):
     eng = _engine(geom, "cc-pvdz", "angstrom")
     D = torch.tensor(_random_density(eng.nbf, 7), dtype=torch.float64, device="cuda")
     res = {}
-    for per_sm in (0, engine.KET_SPLIT_PER_SM):
+    for per_sm in (0, 256):
         monkeypatch.setattr(engine, "KET_SPLIT_PER_SM", per_sm)
         eng._quartet_cache.clear()
         ql = eng.quartets(1e-12)
         res[per_sm] = (ql.class_counts(), [x.cpu().numpy() for x in eng.jk(D, 1e-12, "fp64")],
                        [x.cpu().numpy() for x in eng.jk(D, 1e-12, "mixed_prim", 1e-3)])
-    (c0, jk0, jp0), (c1, jk1, jp1) = res[0], res[engine.KET_SPLIT_PER_SM]
+    (c0, jk0, jp0), (c1, jk1, jp1) = res[0], res[256]
     assert sum(c1[12:19]) > sum(c0[12:19]) and (c1[:12] == c0[:12]).all()
     for a, b in zip(jk0, jk1):
         np.testing.assert_allclose(b, a, atol=1e-12)
