@@ -14,9 +14,12 @@ Checked here:
   projections J @ R, K @ R onto 8 seeded random vectors (1e-9: each is a sum of
   nbf terms whose elements agree to ~1e-11), their diagonals (1e-10) and the
   one-build energy E(D) = 1/2 tr D (H + F(D)) (1e-8 Eh);
-* the energy error of the mixed-precision builds against the oracle at the
-  bounds 1e-3, 1e-4 and 1e-5 (one build at the converged density: <= 1e-6 Eh),
-  and of a mixed SCF, which finishes in FP64 (<= 1e-8 Eh).
+* the energy error of the mixed-precision builds ("mixed", "mixed_prim" and
+  the headline's "mixed_df") against the oracle at the bounds 1e-3, 1e-4 and
+  1e-5 (one build at the converged density: <= 1e-6 Eh), and of a mixed SCF,
+  which finishes in FP64 (double-float for "mixed_df") (<= 1e-8 Eh);
+* the double-float build "df64" at the oracle density: J and K as for FP64,
+  and its SCF energy (1e-8 Eh).
 """
 
 import os
@@ -70,10 +73,11 @@ def _energy_at(eng, H, D, precision, tau=1e-4):
     return float(0.5 * torch.sum(D * (H + F)))
 
 
+@pytest.mark.parametrize("precision", ["fp64", "df64"])
 @pytest.mark.parametrize("name", ["headline_c2", "headline_c3"])
-def test_fp64_jk_at_oracle_density(gpu_lib, name):
+def test_accurate_jk_at_oracle_density(gpu_lib, name, precision):
     g, mol, eng, S, T, V, D, R = _setup(name)
-    J, K = eng.jk(D, SCREEN, "fp64")
+    J, K = eng.jk(D, SCREEN, precision)
     J, K = J.cpu().numpy(), K.cpu().numpy()
     np.testing.assert_allclose(J @ R, g["JR"], rtol=0, atol=1e-9)
     np.testing.assert_allclose(K @ R, g["KR"], rtol=0, atol=1e-9)
@@ -82,23 +86,24 @@ def test_fp64_jk_at_oracle_density(gpu_lib, name):
     Dn = D.cpu().numpy()
     assert abs(np.sum(Dn * J) - float(g["trDJ"])) < 1e-8
     assert abs(np.sum(Dn * K) - float(g["trDK"])) < 1e-8
-    assert abs(_energy_at(eng, T + V, D, "fp64") - float(g["E_at_D"])) < 1e-8
+    assert abs(_energy_at(eng, T + V, D, precision) - float(g["E_at_D"])) < 1e-8
 
 
+@pytest.mark.parametrize("precision", ["fp64", "df64"])
 @pytest.mark.parametrize("name", ["headline_c2", "headline_c3"])
-def test_fp64_scf_energy_matches_oracle(gpu_lib, name):
+def test_accurate_scf_energy_matches_oracle(gpu_lib, name, precision):
     from slowquant_gb300.hartreefock import DirectJK, run_hartree_fock
     from slowquant_gb300.logger import _Logger
 
     g, mol, eng, S, T, V, D, R = _setup(name)
     log = _Logger()
     log.print_output = False
-    E, _, _, _ = run_hartree_fock(S, T, V, DirectJK(eng, SCREEN, "fp64"), mol.number_electrons, log, 1e-9, 1e-9,
-                                  100, True)
+    E, _, _, _ = run_hartree_fock(S, T, V, DirectJK(eng, SCREEN, precision), mol.number_electrons, log, 1e-9,
+                                  1e-9, 100, True)
     assert abs(E - float(g["E_hf"])) < 1e-8, E - float(g["E_hf"])
 
 
-@pytest.mark.parametrize("precision", ["mixed", "mixed_prim"])
+@pytest.mark.parametrize("precision", ["mixed", "mixed_prim", "mixed_df"])
 @pytest.mark.parametrize("tau", [1e-3, 1e-4, 1e-5])
 def test_mixed_one_build_energy_error_vs_oracle(gpu_lib, precision, tau):
     g, mol, eng, S, T, V, D, R = _setup("headline_c3")
@@ -106,7 +111,7 @@ def test_mixed_one_build_energy_error_vs_oracle(gpu_lib, precision, tau):
     assert abs(dE) <= 1e-6, (precision, tau, dE)
 
 
-@pytest.mark.parametrize("precision", ["mixed", "mixed_prim"])
+@pytest.mark.parametrize("precision", ["mixed", "mixed_prim", "mixed_df"])
 def test_mixed_scf_energy_vs_oracle(gpu_lib, precision):
     from slowquant_gb300.hartreefock import DirectJK, run_hartree_fock
     from slowquant_gb300.logger import _Logger
@@ -114,7 +119,7 @@ def test_mixed_scf_energy_vs_oracle(gpu_lib, precision):
     g, mol, eng, S, T, V, D, R = _setup("headline_c3")
     log = _Logger()
     log.print_output = False
-    jk = DirectJK(eng, SCREEN, precision, 1e-4, 1e-5)
+    jk = DirectJK(eng, SCREEN, precision, 1e-3 if precision == "mixed_df" else 1e-4, 1e-5)
     E, _, _, _ = run_hartree_fock(S, T, V, jk, mol.number_electrons, log, 1e-9, 1e-9, 100, True)
-    assert jk.builds[0] == precision and jk.builds[-1] == "fp64"
+    assert jk.builds[0] == precision and jk.builds[-1] == ("df64" if precision == "mixed_df" else "fp64")
     assert abs(E - float(g["E_hf"])) < 1e-8, E - float(g["E_hf"])
