@@ -733,38 +733,43 @@ def batch_arm(args) -> None:
         torch.cuda.synchronize()
         return E, (time.time() - t0) / steps
 
-    for prec in ("fp64", "mixed"):
+    # FP64 and mixed, and the same with double-float arithmetic in place of FP64
+    taus = {"fp64": 1e-4, "mixed": 1e-4, "df64": 1e-4, "mixed_df": 1e-4}
+    for prec in ("fp64", "mixed", "df64", "mixed_df"):
         t0 = time.time()
-        scf = BatchSCF(be, prec)
+        scf = BatchSCF(be, prec, fp32_threshold=taus[prec])
         torch.cuda.synchronize()
         prep_s = time.time() - t0
         E, scf_s = timed_runs(scf)
-        mode = "fp64" if prec == "fp64" else "mixed"
+        mode = "fp64" if prec in ("fp64", "df64") else "mixed"
         ms_fock = float(np.median(time_events(torch, lambda: scf.fock(mode), 5)))
         # the same SCF with the built-in launch shapes, and with eager iterations (no graphs)
         autotune.reset()
-        _, scf_default_s = timed_runs(BatchSCF(be, prec))
-        _, scf_eager_s = timed_runs(BatchSCF(be, prec, use_graphs=False))
+        _, scf_default_s = timed_runs(BatchSCF(be, prec, fp32_threshold=taus[prec]))
+        _, scf_eager_s = timed_runs(BatchSCF(be, prec, fp32_threshold=taus[prec], use_graphs=False))
         autotune.apply(tuning)
         res[prec] = {"molecules_per_s": len(mols) / scf_s, "scf_s": scf_s,
                      "per_molecule_scf_ms": scf_s * 1e3 / len(mols), "iterations": scf.iterations,
                      "host_syncs_per_scf": scf.host_syncs, "fock_build_ms": ms_fock,
                      "molecules_per_s_default_launch_shapes": len(mols) / scf_default_s,
                      "molecules_per_s_eager_iterations": len(mols) / scf_eager_s,
-                     "list_prep_s": round(prep_s, 2), "E": E}
-    dE = float(np.max(np.abs(res["mixed"]["E"] - res["fp64"]["E"])))
+                     "list_prep_s": round(prep_s, 2), "fp32_threshold": taus[prec], "E": E}
+    dE = {p: float(np.max(np.abs(res[p]["E"] - res["fp64"]["E"]))) for p in ("mixed", "df64", "mixed_df")}
     for r in res.values():
         r.pop("E")
     line = {
-        "metric": "molecules/s, batched RHF (FP64 vs mixed)", "value": res["mixed"]["molecules_per_s"],
+        "metric": "molecules/s, batched RHF (FP64 vs mixed)", "value": res["mixed_df"]["molecules_per_s"],
         "unit": "molecules/s", "n_gpus": 1, "steps": max(1, min(args.steps, 3)), "warmup": 1,
-        "ms_per_step": res["mixed"]["scf_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64+f32 (mixed)", "data": "synthetic",
+        "ms_per_step": res["mixed_df"]["scf_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "df64+f32 (mixed_df)", "data": "synthetic",
+        "precision_mode": "mixed_df (quartets with bound below 1e-4 in FP32, the others in double-float; "
+                          "the SCF ends in double-float)",
         "config": {"workload": f"{len(mols)} water clusters (H2O)_k, k~U{{1..6}} (seed 256), 6-31G*, full RHF SCF",
                    "total_bf": int(sum(m.number_bf for m in mols)), "waters": int(sizes.sum()),
                    "step": "one batched SCF to convergence (dE, rmsD < 1e-9) of every molecule, each iteration "
                            "replayed from a CUDA graph"},
-        "fp64": res["fp64"], "mixed": res["mixed"], "max_abs_dE_mixed_vs_fp64": dE,
+        "fp64": res["fp64"], "mixed": res["mixed"], "df64": res["df64"], "mixed_df": res["mixed_df"],
+        "max_abs_dE_mixed_vs_fp64": dE["mixed"], "max_abs_dE_vs_fp64": dE,
         "setup_s": round(setup_s, 2), "autotune_s": round(tune_s, 2),
         "launch_shapes": {f"{c}:{p}": [t, b] for (c, p), (t, b, _) in sorted(tuning.items()) if t},
     }

@@ -332,7 +332,7 @@ int sq_jk_prim(const sq_basis *basis, const sq_pairs *pairs, const sq_slots *slo
  * arithmetic on the FP32 pipe, which GB300 runs at about 60 times its FP64
  * rate; Boys values come from the double-float rows of table32
  * (SQ_BOYS_DF_OFF).  prim_tau splits as in sq_jk_prim (0: every primitive
- * quartet in double-float).  Ddf is caller scratch of 2 * nbf * nbf floats
+ * quartet in double-float; pairs->pq is then not needed).  Ddf is caller scratch of 2 * nbf * nbf floats
  * (mat_total pairs for a packed basis) that the call fills with D as
  * double-float pairs; slots->primdf and slots->hermdf must be written (by
  * sq_slots_fill).  The classes without a double-float kernel run as in

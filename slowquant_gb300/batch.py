@@ -249,6 +249,9 @@ class BatchEngine:
             torch.empty(8 * len(slot_pair), **i32),  # descriptors
             torch.empty(len(slot_pair), dtype=torch.int64, device=dev),  # matrix block offsets
             torch.empty(max(8 * poff, 1), dtype=torch.float32, device=dev) if self.fp32 else None,
+            # double-float (hi, lo) copies for the df64 J/K kernels
+            torch.empty(max(10 * poff, 2), dtype=torch.float32, device=dev) if self.fp32 else None,
+            torch.empty(max(2 * hoff, 2), dtype=torch.float32, device=dev) if self.fp32 else None,
         ]
         t = self.t_slot
         s = SqSlots()
@@ -257,6 +260,7 @@ class BatchEngine:
         s.prim, s.herm, s.prim32, s.herm32 = ptr(t[5]), ptr(t[6]), ptr(t[7]), ptr(t[8])
         s.sub = ptr(t[9])
         s.desc, s.mbase, s.prim32v = ptr(t[10]), ptr(t[11]), ptr(t[12])
+        s.primdf, s.hermdf = ptr(t[13]), ptr(t[14])
         self.slots = s
         fill = SqSlots.from_buffer_copy(s)
         fill.nslot = nslot  # the parents' data only: sub-slots point into it
@@ -338,7 +342,9 @@ class BatchEngine:
         return flat[g.offset:g.offset + len(g.mols) * n * n].view(len(g.mols), n, n)
 
     def jk_accumulate(self, D: torch.Tensor, Jacc: torch.Tensor, Kacc: torch.Tensor, D32: torch.Tensor,
-                      lists, precs) -> None:
+                      lists, precs, prim_tau: float = 0.0) -> None:
+        """sq_jk for each (list, precision); "df64" / "df64_prim" run sq_jk_df (double-float,
+        the latter with the primitive split at prim_tau)."""
         Jacc.zero_()
         Kacc.zero_()
         work = [(ql, prec) for ql, prec in zip(lists, precs) if ql.nquartet]
@@ -355,6 +361,14 @@ class BatchEngine:
         for i, (ql, prec) in enumerate(work):
             st = main if i == 0 else side[i - 1]
             qs = ql.cstruct()
+            if prec in ("df64", "df64_prim"):
+                if getattr(self, "_ddf", None) is None:  # first made in a warm-up call, before any capture
+                    self._ddf = torch.empty(2 * self.mat_total, dtype=torch.float32, device=self.device)
+                check(self.lib.sq_jk_df(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(self.slots),
+                                        ctypes.byref(qs), ptr(self.tab64), ptr(self.tab32), ptr(D), ptr(self._ddf),
+                                        ptr(Jacc), ptr(Kacc), float(prim_tau) if prec == "df64_prim" else 0.0,
+                                        st.cuda_stream), "sq_jk_df")
+                continue
             check(self.lib.sq_jk(ctypes.byref(self.cbasis), ctypes.byref(self.cpairs), ctypes.byref(self.slots),
                                  ctypes.byref(qs), ptr(self.tab64), ptr(self.tab32), ptr(D), ptr(D32), ptr(Jacc),
                                  ptr(Kacc), _lib.PRECISIONS[prec], st.cuda_stream), "sq_jk")
@@ -449,7 +463,9 @@ class _BatchDIIS:
 class BatchSCF:
     """Restricted HF of every molecule of a BatchEngine (hartreefock_in_memory.py:7-94 semantics,
     batched per size group).  precision: "fp64" or "mixed" (FP32 quartets below fp32_threshold
-    until every molecule's DIIS error is below fp64_tail_diis_error, then FP64).
+    until every molecule's DIIS error is below fp64_tail_diis_error, then FP64), and the
+    same two with double-float arithmetic on the FP32 pipe in place of FP64: "df64" and
+    "mixed_df" (quartet-level, as "mixed": the batch carries no primitive Schwarz factors).
 
     With ``use_graphs`` (default) a whole SCF iteration -- the Fock build, DIIS,
     the orthogonalised eigensolve, the new density, the energies and the
@@ -480,10 +496,14 @@ class BatchSCF:
         self.Jacc = torch.zeros_like(self.D)
         self.Kacc = torch.zeros_like(self.D)
         self.D32 = torch.zeros(tot, dtype=torch.float32, device=dev)
-        self.lists = {"fp64": ([be.quartets(threshold)], ["fp64"])}
-        if precision != "fp64":
+        if precision not in ("fp64", "mixed", "df64", "mixed_df"):
+            raise ValueError(f"unknown batch precision {precision!r}")
+        df = precision in ("df64", "mixed_df")
+        # the accurate phase ("fp64") and the mixed phase, in FP64 or double-float
+        self.lists = {"fp64": ([be.quartets(threshold)], ["df64" if df else "fp64"])}
+        if precision in ("mixed", "mixed_df"):
             q64, q32 = be.quartets(threshold, fp32_threshold)
-            self.lists["mixed"] = ([q64, q32], ["fp64", "fp32"])
+            self.lists["mixed"] = ([q64, q32], ["df64" if df else "fp64", "fp32"])
         self.graphs: dict = {}
         self.builds: list[str] = []
         self.tuning: dict = {}
@@ -508,8 +528,10 @@ class BatchSCF:
 
         table = {}
         for mode in self.lists:
-            lists, precs = self.lists[mode]
-            table.update(autotune.tune(run_class, lists, precs, **kw))
+            # double-float launches have no tunable shape
+            pairs = [(ql, p) for ql, p in zip(*self.lists[mode]) if not p.startswith("df")]
+            if pairs:
+                table.update(autotune.tune(run_class, [q for q, _ in pairs], [p for _, p in pairs], **kw))
         self.tuning = table
         self.graphs = {}  # re-capture with the tuned shapes
         self.fock_graphs = {}
@@ -518,7 +540,7 @@ class BatchSCF:
     def _fock_into_F(self, mode: str) -> None:
         be = self.be
         lists, precs = self.lists[mode]
-        be.jk_accumulate(self.D, self.Jacc, self.Kacc, self.D32, lists, precs)
+        be.jk_accumulate(self.D, self.Jacc, self.Kacc, self.D32, lists, precs, self.fp32_threshold)
         for g in be.groups:
             J = be.view(self.Jacc, g)
             K = be.view(self.Kacc, g)
@@ -675,7 +697,7 @@ class BatchSCF:
     def run(self, dE_threshold: float = 1e-9, rmsd_threshold: float = 1e-9, max_iter: int = 100):
         be = self.be
         self._setup_state()
-        mode = "fp64" if self.precision == "fp64" else "mixed"
+        mode = "fp64" if self.precision in ("fp64", "df64") else "mixed"
         self.host_syncs = 0
         for it in range(1, max_iter + 1):
             self._step(mode, dE_threshold, rmsd_threshold)

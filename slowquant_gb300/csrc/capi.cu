@@ -375,9 +375,9 @@ static int jk_common(const char *who, const sq_basis *basis, const sq_pairs *pai
         precision != SQ_DF64)
         return set_error(SQ_ERR_ARG, "%s: unknown precision %d", who, precision);
     if ((precision == SQ_FP64_PRIM || precision == SQ_DF64) &&
-        (!pairs->pq || !slots->prim32v || !slots->herm32 || !table32 || !(prim_tau >= 0.0f)))
-        return set_error(SQ_ERR_ARG, "%s: primitive-level precision needs pairs->pq, FP32 slot data, table32 and a "
-                         "non-negative bound", who);
+        ((prim_tau > 0.0f && !pairs->pq) || !slots->prim32v || !slots->herm32 || !table32 || !(prim_tau >= 0.0f)))
+        return set_error(SQ_ERR_ARG, "%s: primitive-level precision needs FP32 slot data, table32, a non-negative "
+                         "bound and, for a bound above zero, pairs->pq", who);
     if (precision == SQ_DF64 && (!Ddf || !slots->primdf || !slots->hermdf))
         return set_error(SQ_ERR_ARG, "%s: double-float launches need Ddf and slots->primdf, slots->hermdf", who);
     cudaStream_t s = (cudaStream_t)stream;

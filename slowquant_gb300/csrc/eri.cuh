@@ -438,8 +438,10 @@ __device__ __forceinline__ void quartet_block(const EriArgs &args, const SlotDes
         const long long ib = pb + (long long)i * sb;
         const PrimPair<R> br = load_prim<R>(sl, ib);
         if constexpr (SPLIT) {
-            const float thr = args.prim_tau / __ldg(sl.prim32v + 8 * ib + 5);
-            while (K > 0 && __ldg(sl.prim32v + 8 * (kd.pbase + (long long)(K - 1) * kd.pstride) + 5) < thr) --K;
+            if (args.prim_tau > 0.0f) {  // a zero bound keeps every primitive quartet in the accurate arithmetic
+                const float thr = args.prim_tau / __ldg(sl.prim32v + 8 * ib + 5);
+                while (K > 0 && __ldg(sl.prim32v + 8 * (kd.pbase + (long long)(K - 1) * kd.pstride) + 5) < thr) --K;
+            }
         }
         if (!SPLIT || K > 0) {
             R W[LAB + 1][LAB + 1][LAB + 1][NCD];

@@ -71,6 +71,22 @@ def test_batch_mixed_precision(gpu_lib):
     assert np.max(np.abs(Em - E64)) < 1e-6
 
 
+@pytest.mark.parametrize("precision", ["df64", "mixed_df"])
+def test_batch_double_float_modes(gpu_lib, precision):
+    """Double-float arithmetic in place of FP64 on a packed batch: the FP64 batch energies
+    (1e-9 Eh for df64; mixed_df ends in df64 after its mixed phase, 1e-8 Eh)."""
+    from slowquant_gb300.batch import BatchEngine, BatchSCF
+
+    mols = _mols([3, 1, 4, 2])
+    be = BatchEngine(mols)
+    E64 = BatchSCF(be, "fp64").run(1e-10, 1e-10)
+    scf = BatchSCF(be, precision, fp32_threshold=1e-3)
+    E = scf.run(1e-10, 1e-10)
+    if precision == "mixed_df":
+        assert scf.builds[0] == "mixed" and scf.builds[-1] == "fp64"  # the batch's phase names
+    assert np.max(np.abs(E - E64)) < (1e-9 if precision == "df64" else 1e-8)
+
+
 @pytest.mark.parametrize("dims", [[1, 2, 7, 19, 38, 57, 114, 128],  # eigenvectors rotated in global memory
                                   [3, 18, 55, 76, 95, 114, 118]])     # eigenvectors in shared memory
 def test_batched_eigh_ragged_matches_numpy(gpu_lib, dims):
