@@ -678,6 +678,8 @@ def gpu_arm(args) -> None:
             "value": rate, "unit": "quartets/s", "cores": nthreads, "kind": "port",
             "sample": f"{n} uniformly random surviving unique shell quartets of the workload "
                       f"({dt:.1f} s) through the oracle's faithful C restatement of electron_repulsion_integral"}
+    if rank == 0 and args.secondary:
+        line["secondary"] = {"batch": batch_quick(), "gradient": gradient_quick()}
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
@@ -686,6 +688,52 @@ def gpu_arm(args) -> None:
 
 
 # ----------------------------------------------------------------- secondary workloads
+def batch_quick() -> dict:
+    """The batched-SCF workload (256 water clusters, 6-31G*) once in FP64 and once in mixed_df,
+    each after a warm-up run that captures its iteration graphs (the full sweep: --workload batch)."""
+    import torch
+
+    from slowquant_gb300.batch import BatchEngine, BatchSCF
+
+    mols, sizes = _batch_molecules(256)
+    be = BatchEngine(mols)
+    out, E = {}, {}
+    for prec in ("fp64", "mixed_df"):
+        scf = BatchSCF(be, prec)
+        scf.run()
+        torch.cuda.synchronize()
+        t0 = time.time()
+        E[prec] = scf.run()
+        torch.cuda.synchronize()
+        dt = time.time() - t0
+        out[prec] = {"molecules_per_s": len(mols) / dt, "scf_s": round(dt, 3), "iterations": scf.iterations}
+    return {"workload": f"{len(mols)} water clusters (H2O)_k, k~U{{1..6}} (seed 256), 6-31G*, full RHF SCF, "
+                        f"{int(sum(m.number_bf for m in mols))} bf in total",
+            **out, "max_abs_dE_mixed_df_vs_fp64": float(np.max(np.abs(E["mixed_df"] - E["fp64"])))}
+
+
+def gradient_quick() -> dict:
+    """SCF and adjoint RHF gradient of n-octane / cc-pVDZ (the full line with finite-difference checks:
+    --workload gradient)."""
+    import torch
+
+    from slowquant_gb300 import systems
+    from slowquant_gb300.gradient import rhf_gradient, scf_energy
+    from slowquant_gb300.molecule import _Molecule
+
+    m = _Molecule(systems.octane(), 0, "angstrom")
+    m._set_basis_set("cc-pvdz")
+    rhf_gradient(m)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.time()
+    E, D, eng = scf_energy(m)
+    torch.cuda.synchronize()
+    t_scf = time.time() - t0
+    t0 = time.time()
+    g = eng.nuclear_gradient(D, 1e-12)
+    torch.cuda.synchronize()
+    return {"workload": "n-octane cc-pVDZ (210 bf), FP64", "scf_s": round(t_scf, 3),
+            "gradient_s": round(time.time() - t0, 3), "max_abs_grad": float(np.abs(g).max())}
 def _batch_molecules(n: int, seed: int = 256):
     """n seeded water clusters (H2O)_k, k uniform in 1..6, 6-31G*."""
     from slowquant_gb300 import systems
@@ -853,6 +901,8 @@ def main() -> None:
                     help="also time the build with the autotuner's launch shapes for this workload")
     ap.add_argument("--prim-sweep", type=float, nargs="*", default=[1e-4, 1e-3, 1e-2],
                     help="bounds of the primitive-level precision mode reported beside the headline (empty: skip)")
+    ap.add_argument("--no-secondary", dest="secondary", action="store_false",
+                    help="skip the short batched-SCF and gradient measurements appended to the headline line")
     ap.add_argument("--no-df", dest="df", action="store_false",
                     help="skip the double-float (df64, mixed_df) measurements")
     ap.add_argument("--precision", default=HEADLINE, choices=sorted(ACCURATE_LIST),
