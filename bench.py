@@ -565,6 +565,11 @@ def gpu_arm(args) -> None:
     # the launch that carries the most model FLOPs of the build (the longest
     # launches timed alone are short heavy-class lists, which overlap the others)
     big = max(rows, key=lambda r: r["flops"])
+    # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu
+    # capture of the same launch in this workload: the FP64 (dp|dp) launch of the
+    # mixed_df large-bound list at 1e-3, the longest launch of that build
+    ncu_traffic = {("2121", "fp64", "mixed_df", 1e-3, 16, "cc-pvdz"): 4.17e6}
+    traffic = ncu_traffic.get((dom["class"], dom["precision"], HEADLINE, FP32_THR, WATERS, BASIS))
     # The J/K launch also zeroes two nbf^2 accumulators (negligible at 400 bf).
     peak = {"fp64": peak64, "fp32": peak32, "df64": peakdf}[dom["precision"]]
     achieved = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
@@ -641,7 +646,10 @@ def gpu_arm(args) -> None:
                      "achieved": achieved, "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / (peak / 1e12),
                      "peak_source": "measured by sq_fma_probe (FMA loop, in the kernel's arithmetic) in this run",
                      "peaks_tflops": {"fp64": peak64 / 1e12, "df64": peakdf / 1e12, "fp32": peak32 / 1e12},
-                     "traffic": None, "flops_per_launch": dom["flops"], "ms_per_launch": dom["ms"]},
+                     "traffic": traffic,
+                     "traffic_source": None if traffic is None else
+                     "ncu dram__bytes_read.sum + dram__bytes_write.sum, one capture of this launch in this workload",
+                     "flops_per_launch": dom["flops"], "ms_per_launch": dom["ms"]},
         "roofline_by_work": {
             "kernel": f"J/K class ({big['class'][0]}{big['class'][1]}|{big['class'][2]}{big['class'][3]}) "
                       f"{big['precision']}",
