@@ -226,8 +226,9 @@ static cudaError_t launch_class(EriArgs &args, const sq_quartets *qs, int c, int
     if (!warp_fits) return launch_eri_block(args, la, lb, lc, ld, mode, plain, stream);
     // FP32 J/K launches on the warp kernel evaluate each lane's F_m by its own
     // FP32 Taylor expansion: there is no recursion to carry FP32 errors, and the
-    // FP64 expansion (seven DFMAs per lane and primitive quartet) bounded the
-    // f classes' FP32 launches.  The FP32 table reaches m = 10 (the warp kernel: L <= 8).
+    // FP64 expansion (seven DFMAs per lane and primitive quartet) cost the f
+    // classes' FP32 launches about 10 %.  The FP32 table reaches m = 10 (the
+    // warp kernel: L <= 8).
     const int warp_prec = (mode == MODE_JK && plain == SQ_FP32 && L <= SQ_BOYS_NCOL - 1 - kBoysTaylor32)
                               ? SQ_FP32_BOYS32
                               : plain;
