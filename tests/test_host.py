@@ -458,3 +458,30 @@ def test_torch_operators_are_registered_with_shape_rules():
         J, K = torch.ops.slowquant_gb300.direct_jk(1, D, 1e-12, "fp64", 1e-4)
         assert J.shape == (6, 6)
     assert ops.register_engine(object()) >= 1
+
+
+def test_double_float_class_policy():
+    """Which classes an SQ_DF64 launch runs in double-float (host-side dispatch, no device work)."""
+    from slowquant_gb300 import _lib, build
+
+    if not os.path.exists(_lib.LIB_PATH):
+        build.build()
+    L = _lib.lib()
+    big = 1 << 40
+    assert L.sq_get_option(_lib.SQ_OPT_DF_CLASSES) == -1
+    always = (0, 1, 2, 3, 6, 7, 10, 15, 16)
+    long_only = (4, 5, 8, 9, 11)
+    never = (12, 13, 14, 17, 18)
+    for c in always:
+        assert L.sq_df_class(c, 1) == 1 and L.sq_df_class(c, big) == 1
+    for c in long_only:
+        assert L.sq_df_class(c, 1) == 0 and L.sq_df_class(c, big) == 1
+    for c in never + tuple(range(19, _lib.SQ_MAX_QCLASS)) + (-1, _lib.SQ_MAX_QCLASS):
+        assert L.sq_df_class(c, big) == 0
+    try:
+        assert L.sq_set_option(_lib.SQ_OPT_DF_CLASSES, (1 << 12) | (1 << 3) | (1 << 20)) == _lib.SQ_OK
+        assert [c for c in range(19) if L.sq_df_class(c, 1)] == [3, 12]
+        assert L.sq_df_class(20, 1) == 0  # no double-float kernel, whatever the mask
+    finally:
+        L.sq_set_option(_lib.SQ_OPT_DF_CLASSES, -1)
+    assert L.sq_df_class(12, big) == 0
