@@ -253,6 +253,11 @@ int sq_boys_table(double *table64, float *table32, void *stream);
  * (integralfunctions.py:74-97). */
 int sq_boys(int n_max, const double *z, long long nz, const double *table64, int mode, double *out, void *stream);
 
+/* F_0..F_{n_max}(z[i]) (n_max <= 8) as the double-float J/K kernels evaluate
+ * them (Taylor rows at SQ_BOYS_DF_OFF of table32, downward recursion, all in
+ * float pairs), returned as hi + lo in FP64 -> out[nz][n_max+1].  Test hook. */
+int sq_boys_df(int n_max, const double *z, long long nz, const float *table32, double *out, void *stream);
+
 /* Primitive-pair data for every pair in `pairs`: P, p, U and the Hermite
  * expansion coefficients of expansion_coefficients
  * (integralfunctions.py:9-71), times the per-component normalisation of

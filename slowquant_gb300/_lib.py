@@ -149,6 +149,7 @@ def lib() -> ctypes.CDLL:
         L.sq_jk_df.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
                                ctypes.POINTER(SqQuartets), _p, _p, _p, _p, _p, _p, ctypes.c_double, _p]
         L.sq_df_class.argtypes = [ctypes.c_int, ctypes.c_longlong]
+        L.sq_boys_df.argtypes = [ctypes.c_int, _p, ctypes.c_longlong, _p, _p, _p]
         L.sq_jk_noalloc.argtypes = [ctypes.POINTER(SqBasis), ctypes.POINTER(SqPairs), ctypes.POINTER(SqSlots),
                                     ctypes.POINTER(SqQuartets), _p, _p, _p, _p, _p, ctypes.c_int, _p]
         L.sq_fock_build.argtypes = [ctypes.c_int, _p, _p, _p, _p, _p, _p, _p]
@@ -164,7 +165,7 @@ def lib() -> ctypes.CDLL:
 EXPORTED = [
     "sq_version", "sq_last_error", "sq_set_option", "sq_get_option", "sq_set_launch_config", "sq_boys_table", "sq_boys",
     "sq_pair_prep", "sq_schwarz", "sq_eri_dense", "sq_jk", "sq_fock_build", "sq_one_electron",
-    "sq_quartets_expand", "sq_fma_probe", "sq_slots_fill", "sq_slots_describe", "sq_jk_prim", "sq_jk_df", "sq_df_class", "sq_ao2mo_rotate", "sq_multipole", "sq_jk_dense", "sq_jk_noalloc", "sq_grad_2e", "sq_grad_1e",
+    "sq_quartets_expand", "sq_fma_probe", "sq_slots_fill", "sq_slots_describe", "sq_jk_prim", "sq_jk_df", "sq_df_class", "sq_boys_df", "sq_ao2mo_rotate", "sq_multipole", "sq_jk_dense", "sq_jk_noalloc", "sq_grad_2e", "sq_grad_1e",
     "sq_batched_eigh", "sq_jk_multi",
 ]
 

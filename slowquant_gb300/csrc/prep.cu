@@ -82,6 +82,24 @@ __global__ void boys_eval_kernel(int n_max, const double *z, long long nz, const
     for (int m = 0; m <= n_max; ++m) out[i * (n_max + 1) + m] = F[m];
 }
 
+// Double-float Boys (the df64 J/K kernels' boys_df) at FP64 arguments, for the test hook.
+template <int M>
+__global__ void boys_df_eval_kernel(const double *z, long long nz, const float4 *tab, double *out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nz) return;
+    const double v = z[i];
+    const float h = (float)v;
+    dfl F[M + 1];
+    boys_df<M>(dfl(h, (float)(v - (double)h)), tab, F);
+    for (int m = 0; m <= M; ++m) out[i * (M + 1) + m] = (double)F[m].hi + (double)F[m].lo;
+}
+
+template <int M>
+static void launch_boys_df(const double *z, long long nz, const float *table32, double *out, cudaStream_t s) {
+    boys_df_eval_kernel<M><<<(unsigned)((nz + 127) / 128), 128, 0, s>>>(
+        z, nz, reinterpret_cast<const float4 *>(table32 + SQ_BOYS_DF_OFF), out);
+}
+
 // ---------------------------------------------------------------------------
 // Primitive-pair data.  One thread per primitive pair.
 // 1D MD expansion coefficients E^{ij}_t / E^{00}_0 per Cartesian direction
@@ -555,6 +573,26 @@ extern "C" int sq_boys(int n_max, const double *z, long long nz, const double *t
     boys_eval_kernel<<<(unsigned)((nz + 127) / 128), 128, 0, (cudaStream_t)stream>>>(n_max, z, nz, table64, mode,
                                                                                   out);
     return check_launch("sq_boys");
+}
+
+extern "C" int sq_boys_df(int n_max, const double *z, long long nz, const float *table32, double *out,
+                          void *stream) {
+    if (!z || !table32 || !out || nz < 0) return set_error(SQ_ERR_ARG, "sq_boys_df: bad argument");
+    if (n_max < 0 || n_max > 8) return set_error(SQ_ERR_ARG, "sq_boys_df: n_max %d out of range (0..8)", n_max);
+    if (nz == 0) return SQ_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (n_max) {
+        case 0: launch_boys_df<0>(z, nz, table32, out, s); break;
+        case 1: launch_boys_df<1>(z, nz, table32, out, s); break;
+        case 2: launch_boys_df<2>(z, nz, table32, out, s); break;
+        case 3: launch_boys_df<3>(z, nz, table32, out, s); break;
+        case 4: launch_boys_df<4>(z, nz, table32, out, s); break;
+        case 5: launch_boys_df<5>(z, nz, table32, out, s); break;
+        case 6: launch_boys_df<6>(z, nz, table32, out, s); break;
+        case 7: launch_boys_df<7>(z, nz, table32, out, s); break;
+        default: launch_boys_df<8>(z, nz, table32, out, s); break;
+    }
+    return check_launch("sq_boys_df");
 }
 
 extern "C" int sq_pair_prep(const sq_basis *basis, sq_pairs *pairs, void *stream) {

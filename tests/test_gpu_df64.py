@@ -81,6 +81,36 @@ def test_df64_boys_rows_match_fp64_table(gpu_lib):
     assert not df[:, :, 11].any()
 
 
+@pytest.mark.parametrize("n_max", [0, 1, 2, 5, 8])
+def test_double_float_boys_against_fp64_table_and_exact(gpu_lib, n_max):
+    """boys_df (float-pair Taylor rows, downward recursion in float pairs) against the FP64
+    tabulated function (rtol 1e-12, all T) and the exact F_m(T) = 1F1(m+1/2; m+3/2; -T)/(2m+1)
+    (rtol 1e-12 below T = 36, where both expand about the grid; above it both use the
+    same asymptote, whose own error is up to 1e-8 for m = 8 at T = 36)."""
+    import torch
+    from scipy.special import hyp1f1
+
+    from slowquant_gb300 import _lib
+
+    eng = _engine(1, "sto-3g")
+    rng = np.random.default_rng(11)
+    z = np.concatenate([np.arange(0, 60, 1 / 16.0), rng.uniform(0, 60, 4000), [0.0, 1e-9, 35.999, 36.0, 36.001]])
+    zt = torch.tensor(z, dtype=torch.float64, device="cuda")
+    out_df = torch.empty((len(z), n_max + 1), dtype=torch.float64, device="cuda")
+    out64 = torch.empty_like(out_df)
+    L = _lib.lib()
+    s = _lib.stream_handle()
+    _lib.check(L.sq_boys_df(n_max, zt.data_ptr(), len(z), eng.tab32.data_ptr(), out_df.data_ptr(), s), "sq_boys_df")
+    _lib.check(L.sq_boys(n_max, zt.data_ptr(), len(z), eng.tab64.data_ptr(), 0, out64.data_ptr(), s), "sq_boys")
+    Fd, F64 = out_df.cpu().numpy(), out64.cpu().numpy()
+    np.testing.assert_allclose(Fd, F64, rtol=1e-12, atol=0)
+    low = z < 36.0
+    m = np.arange(n_max + 1)
+    exact = hyp1f1(m[None, :] + 0.5, m[None, :] + 1.5, -z[low, None]) / (2 * m[None, :] + 1)
+    np.testing.assert_allclose(Fd[low], exact, rtol=1e-12, atol=0)
+    assert L.sq_boys_df(9, zt.data_ptr(), 1, eng.tab32.data_ptr(), out_df.data_ptr(), s) == _lib.SQ_ERR_ARG
+
+
 @pytest.mark.parametrize("name", ["h2o_sto3g_c1", "ch4_sto3g", "h2o_631gs", "h2o_ccpvdz_c1", "h6_dzp"])
 def test_df64_scf_matches_reference_energies(gpu_lib, golden_energies, name):
     from tests.test_gpu_scf import _run
