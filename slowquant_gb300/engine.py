@@ -546,22 +546,7 @@ class IntegralEngine:
                 want = 1
                 while want < KET_SPLIT_MAX and len(seg) * want < target:
                     want *= 2
-                ket = seg[:, 1].astype(np.int64)
-                whole = ket < self.nslot_base
-                S = np.ones(len(seg), np.int64)
-                first = np.full(len(seg), -1, np.int64)
-                for s in sorted(self.sub_first):
-                    if s > want:
-                        break
-                    f = np.full(len(seg), -1, np.int64)
-                    f[whole] = self.sub_first[s][ket[whole]]
-                    ok = f >= 0
-                    S[ok] = s
-                    first[ok] = f[ok]
-                rep = np.repeat(np.arange(len(seg)), S)
-                j = np.arange(len(rep)) - np.repeat(np.cumsum(S) - S, S)
-                newket = np.where(np.repeat(S, S) > 1, np.repeat(first, S) + j, np.repeat(ket, S))
-                seg = np.stack([seg[rep, 0], newket.astype(np.int32)], axis=1)
+                seg = screening.ket_chunk_entries(seg, self.sub_first, self.nslot_base, want)
             parts.append(seg)
             off[c + 1] = off[c] + len(seg)
         allp = np.concatenate(parts).astype(np.int32) if int(off[-1]) else np.zeros((0, 2), np.int32)

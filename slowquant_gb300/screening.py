@@ -158,6 +158,34 @@ def expand_host(bra, kst, cnt, ket_list) -> np.ndarray:
     return np.stack([rep_bra, ket_list[starts + k]], axis=1).astype(np.int32)
 
 
+def ket_chunk_entries(seg: np.ndarray, sub_first: dict, nslot: int, want: int) -> np.ndarray:
+    """Quartet entries (bra, ket) with each whole ket slot cut into sub-slot chunks.
+
+    For every entry whose ket is a whole slot (id < nslot), S' is the largest
+    chunk count S <= want with sub_first[S][ket] >= 0; the entry becomes S'
+    entries (bra, sub_first[S'][ket] + j), j < S' (chunk j of S' covers the
+    ket's primitive pairs [j n / S', (j+1) n / S')).  Entries without chunks
+    (sub-slot kets, or slots with no chunk table up to want) are kept.  Order:
+    each entry's chunks in place of the entry."""
+    seg = np.asarray(seg, dtype=np.int64).reshape(-1, 2)
+    ket = seg[:, 1]
+    whole = ket < nslot
+    S = np.ones(len(seg), np.int64)
+    first = np.full(len(seg), -1, np.int64)
+    for s in sorted(sub_first):
+        if s > want:
+            break
+        f = np.full(len(seg), -1, np.int64)
+        f[whole] = np.asarray(sub_first[s])[ket[whole]]
+        ok = f >= 0
+        S[ok] = s
+        first[ok] = f[ok]
+    rep = np.repeat(np.arange(len(seg)), S)
+    j = np.arange(len(rep)) - np.repeat(np.cumsum(S) - S, S)
+    newket = np.where(np.repeat(S, S) > 1, np.repeat(first, S) + j, np.repeat(ket, S))
+    return np.stack([seg[rep, 0], newket], axis=1).astype(np.int32)
+
+
 def sub_slot_table(npp, pbase, pstride, hbase, herm_per_prim, weight, qcum, prim_off, max_np: int,
                    split_target: float, min_chunk: int = 4):
     """Sub-slots: chunk k of S (a power of two) of a slot's primitive pairs.

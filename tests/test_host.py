@@ -485,3 +485,19 @@ def test_double_float_class_policy():
     finally:
         L.sq_set_option(_lib.SQ_OPT_DF_CLASSES, -1)
     assert L.sq_df_class(12, big) == 0
+
+
+def test_ket_chunk_entries_cut_whole_kets_only():
+    """screening.ket_chunk_entries: each whole ket with chunks becomes its chunks, in place; others stay."""
+    from slowquant_gb300 import screening
+
+    nslot = 5
+    # chunk tables: S = 2 for slots 1, 3; S = 4 for slot 3 only (ids continue after the slots)
+    sub_first = {2: np.array([-1, 5, -1, 7, -1]), 4: np.array([-1, -1, -1, 9, -1])}
+    seg = np.array([[0, 1], [2, 3], [4, 0], [1, 8]], dtype=np.int32)  # the last ket is a sub-slot already
+    out = screening.ket_chunk_entries(seg, sub_first, nslot, want=4)
+    assert out.tolist() == [[0, 5], [0, 6], [2, 9], [2, 10], [2, 11], [2, 12], [4, 0], [1, 8]]
+    out2 = screening.ket_chunk_entries(seg, sub_first, nslot, want=2)
+    assert out2.tolist() == [[0, 5], [0, 6], [2, 7], [2, 8], [4, 0], [1, 8]]
+    assert screening.ket_chunk_entries(seg, sub_first, nslot, want=1).tolist() == seg.tolist()
+    assert screening.ket_chunk_entries(np.zeros((0, 2), np.int32), sub_first, nslot, 4).shape == (0, 2)
